@@ -1,0 +1,98 @@
+"""ctypes binding of libchorus_gpu.so (the C-ABI declared in include/chorus_gpu.h).
+
+The shared library is built in-tree by ``chorus-mhd_gb300/build.py``.  There is no
+CPU fallback: if the library is missing or cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libchorus_gpu.so")
+
+c_int, c_double, c_char_p, c_void_p = ctypes.c_int32, ctypes.c_double, ctypes.c_char_p, ctypes.c_void_p
+P = ctypes.POINTER
+dp, ip = P(c_double), P(c_int)
+
+
+class ChorusDims(ctypes.Structure):
+    _fields_ = [("N", c_int), ("NCELL", c_int), ("NFACE", c_int), ("NINTER", c_int), ("NFREE", c_int),
+                ("NPAIR", c_int)]
+
+
+class ChorusParams(ctypes.Structure):
+    _fields_ = [("gam", c_double), ("mu", c_double), ("eta0", c_double), ("DXCYCL", c_double),
+                ("DYCYCL", c_double), ("dt", c_double), ("B0x", c_double), ("B0y", c_double),
+                ("NCELLGLOB", c_int), ("vismode", c_int), ("ARTIV", c_int), ("k_stage", c_int)]
+
+
+class ChorusDiag(ctypes.Structure):
+    _fields_ = [("iter", c_int), ("pad", c_int), ("ctime", c_double), ("residglob", c_double),
+                ("divBglob", c_double), ("eigvmax_g", c_double), ("epsilon0", c_double)]
+
+
+# name -> (restype, argtypes); every function of include/chorus_gpu.h
+SIGNATURES = {
+    "chorus_gpu_last_error": (c_char_p, []),
+    "chorus_gpu_version": (c_char_p, []),
+    "chorus_gpu_bind": (c_int, [P(ChorusDims), ip, ip, ip, ip, ip, ip, dp, dp, dp, dp, dp, dp, dp,
+                                P(ChorusParams), c_int, P(c_void_p)]),
+    "chorus_gpu_free": (c_int, [c_void_p]),
+    "chorus_gpu_set_params": (c_int, [c_void_p, P(ChorusParams)]),
+    "chorus_gpu_upload_state": (c_int, [c_void_p, dp]),
+    "chorus_gpu_download_state": (c_int, [c_void_p, dp]),
+    "chorus_gpu_download_array": (c_int, [c_void_p, c_char_p, dp, ctypes.c_int64]),
+    "chorus_gpu_get_eigvmax": (c_int, [c_void_p, dp, dp]),
+    "compresid_gpu": (c_int, [c_void_p]),
+    "comp_inviscid_flux_gpu": (c_int, [c_void_p]),
+    "nablaqsp_gpu": (c_int, [c_void_p, ip, ip]),
+    "correct_b_via_curl_az_gpu": (c_int, [c_void_p]),
+    "rk_s5p3_gpu": (c_int, [c_void_p, dp]),
+    "fivestagerk_gpu": (c_int, [c_void_p, dp]),
+    "iterations_gpu": (c_int, [c_void_p, c_int, ip, dp, P(ChorusDiag), c_int, ip]),
+    "getrusanovflux_gpu": (c_int, [c_int, c_double, dp, dp, dp, dp, dp, dp, ip, ip, dp]),
+    "getifluxvectors_gpu": (c_int, [c_int, c_double, dp, dp, dp]),
+    "getvfluxvectors_gpu": (c_int, [c_int, c_double, c_double, c_double, dp, dp, dp, dp]),
+    "chorus_mesh_load": (c_int, [c_char_p, P(c_void_p)]),
+    "chorus_mesh_free": (c_int, [c_void_p]),
+    "chorus_mesh_info": (c_int, [c_void_p, P(ChorusDims), P(ChorusParams), ip, ip]),
+    "chorus_mesh_iarray": (ip, [c_void_p, c_char_p, P(ctypes.c_int64)]),
+    "chorus_mesh_darray": (dp, [c_void_p, c_char_p, P(ctypes.c_int64)]),
+    "chorus_gpu_bind_mesh": (c_int, [c_void_p, c_int, P(c_void_p)]),
+    "chorus_initial_state": (c_int, [c_void_p, c_void_p, dp]),
+    "chorus_write_restart": (c_int, [c_void_p, c_char_p, c_int, c_double]),
+    "chorus_read_restart": (c_int, [c_void_p, c_char_p, ip, dp]),
+}
+
+_lib = None
+
+
+class ChorusError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("chorus error %d: %s" % (code, msg))
+        self.code = code
+
+
+def load(path: str | None = None):
+    """Load the in-tree library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libchorus_gpu.so is not built (%s); run chorus-mhd_gb300/build.py" % p)
+    L = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != 0:
+        raise ChorusError(rc, load().chorus_gpu_last_error().decode())
+    return rc

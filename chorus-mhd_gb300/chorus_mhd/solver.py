@@ -1,0 +1,192 @@
+"""Host-side mirror of the reference's hot-path interface.
+
+``Mesh`` wraps the library's setup chain (QUAD.INP + .CEL/.VRT/.BND -> the reference's
+maps and geometry).  ``Solver`` binds a mesh to one GPU and exposes the reference
+routines by their names -- ``compresid``, ``comp_inviscid_flux``, ``nablaQsp``,
+``correct_B_via_curl_Az``, ``RK_S5P3``, ``FiveStageRk``, ``iterations`` -- operating on
+the device-resident state.  Arrays come back in the reference's Fortran layout,
+flattened (first index fastest).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import ChorusDiag, ChorusDims, ChorusParams, check
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+class Mesh:
+    """The reference's setup chain for one case directory (readinput ... calcjacob)."""
+
+    def __init__(self, case_dir: str):
+        self.L = _lib.load()
+        h = ctypes.c_void_p()
+        check(self.L.chorus_mesh_load(case_dir.encode(), ctypes.byref(h)))
+        self._h = h
+        self.case_dir = case_dir
+        self.dims = ChorusDims()
+        self.params = ChorusParams()
+        mi, pb = ctypes.c_int32(), ctypes.c_int32()
+        check(self.L.chorus_mesh_info(self._h, ctypes.byref(self.dims), ctypes.byref(self.params),
+                                      ctypes.byref(mi), ctypes.byref(pb)))
+        self.maxiter, self.problem = mi.value, pb.value
+
+    @property
+    def N(self):
+        return self.dims.N
+
+    @property
+    def ncell(self):
+        return self.dims.NCELL
+
+    def iarray(self, name) -> np.ndarray:
+        n = ctypes.c_int64()
+        p = self.L.chorus_mesh_iarray(self._h, name.encode(), ctypes.byref(n))
+        if not p:
+            raise KeyError(name)
+        return np.ctypeslib.as_array(p, shape=(n.value,)).copy() if n.value else np.zeros(0, np.int32)
+
+    def darray(self, name) -> np.ndarray:
+        n = ctypes.c_int64()
+        p = self.L.chorus_mesh_darray(self._h, name.encode(), ctypes.byref(n))
+        if not p:
+            raise KeyError(name)
+        return np.ctypeslib.as_array(p, shape=(n.value,)).copy() if n.value else np.zeros(0)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.chorus_mesh_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """One solve resident on one GPU; method names follow the reference routines."""
+
+    def __init__(self, mesh: Mesh, device: int = 0, initial_state: bool = True):
+        self.L = _lib.load()
+        self.mesh = mesh
+        ctx = ctypes.c_void_p()
+        check(self.L.chorus_gpu_bind_mesh(mesh._h, device, ctypes.byref(ctx)))
+        self._ctx = ctx
+        self.N, self.ncell = mesh.N, mesh.ncell
+        self.nq = 9 * self.N * self.N * self.ncell
+        self.iter = 0
+        self.ctime = 0.0
+        self.diagnostics: list[dict] = []
+        if initial_state:
+            self.set_initial_state()
+
+    # ---- state
+    def set_initial_state(self) -> np.ndarray:
+        Q = np.empty(self.nq)
+        check(self.L.chorus_initial_state(self.mesh._h, self._ctx, _dp(Q)))
+        self.iter, self.ctime = 0, 0.0
+        return Q
+
+    def upload(self, Q: np.ndarray):
+        Q = np.ascontiguousarray(Q, np.float64).reshape(-1)
+        assert Q.size == self.nq
+        check(self.L.chorus_gpu_upload_state(self._ctx, _dp(Q)))
+
+    def state(self) -> np.ndarray:
+        Q = np.empty(self.nq)
+        check(self.L.chorus_gpu_download_state(self._ctx, _dp(Q)))
+        return Q
+
+    def array(self, name: str, count: int) -> np.ndarray:
+        out = np.empty(count)
+        check(self.L.chorus_gpu_download_array(self._ctx, name.encode(), _dp(out), count))
+        return out
+
+    def eigvmax(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        check(self.L.chorus_gpu_get_eigvmax(self._ctx, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def set_params(self, **kw):
+        p = ChorusParams.from_buffer_copy(self.mesh.params)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        check(self.L.chorus_gpu_set_params(self._ctx, ctypes.byref(p)))
+
+    # ---- reference routines
+    def compresid(self):
+        check(self.L.compresid_gpu(self._ctx))
+
+    def comp_inviscid_flux(self):
+        check(self.L.comp_inviscid_flux_gpu(self._ctx))
+
+    def nablaQsp(self, v_sta: int, v_end: int):
+        a, b = ctypes.c_int32(v_sta), ctypes.c_int32(v_end)
+        check(self.L.nablaqsp_gpu(self._ctx, ctypes.byref(a), ctypes.byref(b)))
+
+    def correct_B_via_curl_Az(self):
+        check(self.L.correct_b_via_curl_az_gpu(self._ctx))
+
+    def RK_S5P3(self):
+        t = ctypes.c_double(self.ctime)
+        check(self.L.rk_s5p3_gpu(self._ctx, ctypes.byref(t)))
+        self.ctime = t.value
+
+    def FiveStageRk(self):
+        t = ctypes.c_double(self.ctime)
+        check(self.L.fivestagerk_gpu(self._ctx, ctypes.byref(t)))
+        self.ctime = t.value
+
+    def iterations(self, nsteps: int) -> list[dict]:
+        """nsteps of iterations.f90:19-87 (RK step, CT projection, norms every 10)."""
+        it = ctypes.c_int32(self.iter)
+        t = ctypes.c_double(self.ctime)
+        cap = nsteps // 10 + 2
+        recs = (ChorusDiag * cap)()
+        nd = ctypes.c_int32(0)
+        check(self.L.iterations_gpu(self._ctx, int(nsteps), ctypes.byref(it), ctypes.byref(t), recs, cap,
+                                    ctypes.byref(nd)))
+        self.iter, self.ctime = it.value, t.value
+        out = [dict(iter=r.iter, ctime=r.ctime, residglob=r.residglob, divBglob=r.divBglob,
+                    eigvmax_g=r.eigvmax_g, epsilon0=r.epsilon0) for r in recs[: min(nd.value, cap)]]
+        self.diagnostics.extend(out)
+        return out
+
+    def write_restart(self, path: str):
+        check(self.L.chorus_write_restart(self._ctx, path.encode(), self.iter, self.ctime))
+
+    def read_restart(self, path: str):
+        it, t = ctypes.c_int32(), ctypes.c_double()
+        check(self.L.chorus_read_restart(self._ctx, path.encode(), ctypes.byref(it), ctypes.byref(t)))
+        self.iter, self.ctime = it.value, t.value
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self.L.chorus_gpu_free(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def reference_layout_sizes(N: int, ncell: int) -> dict:
+    """Element counts of the reference's work arrays (for download_array)."""
+    ns, nf = N * N * ncell, (N + 1) * N * ncell
+    return {"Q": 9 * ns, "resid": 9 * ns, "F1": 8 * nf, "G2": 8 * nf, "Qvfi": 9 * nf, "Qvfj": 9 * nf,
+            "Azfi": nf, "Azfj": nf, "nablaQs": 18 * ns, "nablaQvfi": 18 * nf, "nablaQvfj": 18 * nf,
+            "nablaAs": 2 * ns, "muAVfi": 18 * ncell, "muAVfj": 18 * ncell, "SM_IND1": ncell}

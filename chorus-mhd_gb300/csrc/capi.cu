@@ -1,0 +1,961 @@
+// capi.cu -- the C-ABI of libchorus_gpu.so: context binding, resident state, the
+// drop-in entry points for the reference routines, CUDA-graph step replay, parity
+// downloads and the host-side setup entry points.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "chorus_internal.h"
+#include "kernels.cuh"
+
+namespace chorus {
+
+// upload functions defined in kernels_n*.cu (each TU owns its constant operators)
+void upload_ops_n2(const OpsN&);
+void upload_ops_n3(const OpsN&);
+void upload_ops_n4(const OpsN&);
+void upload_ops_n5(const OpsN&);
+void upload_ops_n6(const OpsN&);
+void upload_ops_n7(const OpsN&);
+void upload_ops_n8(const OpsN&);
+void launch_e1_nosensor_n2(const SolveDev&, const Launch&, cudaStream_t);
+void launch_e1_nosensor_n3(const SolveDev&, const Launch&, cudaStream_t);
+void launch_e1_nosensor_n4(const SolveDev&, const Launch&, cudaStream_t);
+void launch_e1_nosensor_n5(const SolveDev&, const Launch&, cudaStream_t);
+void launch_e1_nosensor_n6(const SolveDev&, const Launch&, cudaStream_t);
+void launch_e1_nosensor_n7(const SolveDev&, const Launch&, cudaStream_t);
+void launch_e1_nosensor_n8(const SolveDev&, const Launch&, cudaStream_t);
+
+static thread_local std::string g_err;
+
+int set_err(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                               \
+  do {                                                                                         \
+    cudaError_t _e = (call);                                                                   \
+    if (_e != cudaSuccess)                                                                     \
+      return set_err(CHORUS_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// operators in constant memory, once per (device, N)
+// ---------------------------------------------------------------------------
+static std::mutex g_ops_mu;
+static bool g_ops_done[64][kMaxN + 1];
+
+static void make_ops(int N, const double* Lmat, const double* Mmat, const double* Xs, const double* Xf, OpsN& o) {
+  std::memset(&o, 0, sizeof o);
+  for (int i = 0; i < (N + 1) * N; i++) { o.L[i] = Lmat[i]; o.M[i] = Mmat[i]; }
+  for (int i = 0; i <= N; i++) o.Xf[i] = Xf[i];
+  for (int i = 0; i < N; i++) o.Xs[i] = Xs[i];
+  // AV smoothing A = Hlow * H: project N points onto the N-1 low-order points
+  // (hhval at Xs_low, AV.f90:19-35) and evaluate back (hhval_low at Xs, :41-58)
+  double xsl[kMaxN], xfl[kMaxN + 1];
+  setsandpoints(N - 1, xsl, xfl);
+  for (int i = 0; i < N; i++)
+    for (int m = 0; m < N; m++) {
+      double a = 0.0;
+      for (int l = 0; l < N - 1; l++) a += lagrange(xsl, N - 1, l, Xs[i]) * lagrange(Xs, N, m, xsl[l]);
+      o.A[i * N + m] = a;
+    }
+}
+
+static int ensure_ops(int dev, int N, const double* Lmat, const double* Mmat, const double* Xs, const double* Xf) {
+  std::lock_guard<std::mutex> lk(g_ops_mu);
+  if (dev >= 0 && dev < 64 && g_ops_done[dev][N]) return CHORUS_OK;
+  OpsN o;
+  make_ops(N, Lmat, Mmat, Xs, Xf, o);
+  switch (N) {
+    case 2: upload_ops_n2(o); break;
+    case 3: upload_ops_n3(o); break;
+    case 4: upload_ops_n4(o); break;
+    case 5: upload_ops_n5(o); break;
+    case 6: upload_ops_n6(o); break;
+    case 7: upload_ops_n7(o); break;
+    case 8: upload_ops_n8(o); break;
+    default: return set_err(CHORUS_EINVAL, "N=%d not supported", N);
+  }
+  CK(cudaGetLastError());
+  if (dev >= 0 && dev < 64) g_ops_done[dev][N] = true;
+  return CHORUS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// per-N dispatch of the stage launches
+// ---------------------------------------------------------------------------
+struct Dispatch {
+  void (*e1)(const SolveDev&, const Launch&, cudaStream_t);
+  void (*e1ns)(const SolveDev&, const Launch&, cudaStream_t);
+  void (*f1)(const SolveDev&, cudaStream_t);
+  void (*e2)(const SolveDev&, const Launch&, cudaStream_t);
+  void (*f2)(const SolveDev&, cudaStream_t);
+  void (*e3)(const SolveDev&, const RKStage&, const Launch&, cudaStream_t);
+  void (*ct)(const SolveDev&, const Launch&, cudaStream_t, int);
+  void (*nqsp)(const SolveDev&, int, int, cudaStream_t);
+  void (*divb)(const SolveDev&, cudaStream_t);
+};
+#define DISPATCH(n) \
+  Dispatch{launch_e1<n>, launch_e1_nosensor_n##n, launch_f1<n>, launch_e2<n>, launch_f2<n>, launch_e3<n>, launch_ct<n>, launch_nqsp<n>, launch_divb<n>}
+static const Dispatch* dispatch_for(int N) {
+  static const Dispatch d[kMaxN + 1] = {Dispatch{}, Dispatch{}, DISPATCH(2), DISPATCH(3), DISPATCH(4),
+                                        DISPATCH(5), DISPATCH(6), DISPATCH(7), DISPATCH(8)};
+  return (N >= kMinN && N <= kMaxN) ? &d[N] : nullptr;
+}
+
+// default launch shapes per N (cells per CTA, threads per CTA)
+Launch default_launch(int N, int which) {
+  // which: 0 = E1, 1 = E2, 2 = E3, 3 = CT
+  static const int epb[kMaxN + 1][4] = {{0}, {0}, {16, 16, 16, 16}, {8, 8, 8, 8}, {8, 6, 8, 8},
+                                        {4, 4, 4, 4}, {4, 2, 4, 4}, {2, 2, 2, 2}, {2, 2, 2, 2}};
+  return Launch{epb[N][which], 128};
+}
+
+}  // namespace chorus
+
+using namespace chorus;
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct ChorusCtx {
+  int device = 0;
+  ChorusDims dims{};
+  ChorusParams p{};
+  int nface2 = 0, nface1 = 0;
+  cudaStream_t st = nullptr;
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  SolveDev sd{};
+  double* red = nullptr;       // [4]: diag sums, eig as double
+  double* h_pinned = nullptr;  // pinned staging for diag records
+  Launch L[4];
+  cudaGraphExec_t g_step = nullptr, g_diag = nullptr;
+  double graph_dt = NAN;
+  int graph_k = -1;
+  const Dispatch* D = nullptr;
+};
+
+static int ctx_device(ChorusCtx* c) {
+  CK(cudaSetDevice(c->device));
+  return CHORUS_OK;
+}
+
+struct ArenaPlan {
+  size_t off = 0;
+  template <typename T>
+  size_t take(size_t count) {
+    size_t o = off;
+    off += ((count * sizeof(T) + 255) / 256) * 256;
+    return o;
+  }
+};
+
+extern "C" {
+
+const char* chorus_gpu_last_error(void) { return g_err.c_str(); }
+const char* chorus_gpu_version(void) { return "chorus-gb300 0.1 (sm_103a, FP64)"; }
+
+int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* IBFINTER, const int32_t* IBFREE,
+                    const int32_t* CYC2FPAIR, const int32_t* iface2fp, const int32_t* jface2fp, const double* Xs,
+                    const double* Xf, const double* Lmat, const double* Mmat, const double* S1, const double* S2,
+                    const double* Jac, const ChorusParams* params, int32_t device, ChorusCtx** out) {
+  if (!dims || !params || !out || !Xs || !Xf || !Lmat || !Mmat || !S1 || !S2 || !Jac || !IF2C)
+    return set_err(CHORUS_EINVAL, "chorus_gpu_bind: null argument");
+  *out = nullptr;
+  const int N = dims->N, NC = dims->NCELL, NF = dims->NFACE;
+  if (N < kMinN || N > kMaxN) return set_err(CHORUS_EINVAL, "N=%d outside %d..%d", N, kMinN, kMaxN);
+  if (NC <= 0 || NF <= 0 || dims->NINTER < 0 || dims->NFREE < 0 || dims->NPAIR < 0)
+    return set_err(CHORUS_EINVAL, "bad dims (NCELL=%d NFACE=%d)", NC, NF);
+  if ((dims->NINTER && !IBFINTER) || (dims->NFREE && !IBFREE) || (dims->NPAIR && !CYC2FPAIR))
+    return set_err(CHORUS_EINVAL, "face list pointer is null");
+  if (params->vismode != 1)
+    return set_err(CHORUS_EINVAL, "vismode must be 1 (Qvfi/Azfi are written only when vismode==1)");
+  if (params->k_stage != 3 && params->k_stage != 5)
+    return set_err(CHORUS_EINVAL, "k_stage can be only 3 or 5");
+  if ((int64_t)NC * 2 * (N + 1) * N * 18 > ((int64_t)1 << 40))
+    return set_err(CHORUS_EINVAL, "mesh too large");
+  // face2fpconnec must be the reference's (initsetup.f90:343-379); the kernels
+  // hard-code it
+  if (iface2fp && jface2fp)
+    for (int nfp = 1; nfp <= N; nfp++) {
+      const int ei[4] = {nfp, N + 1, N - nfp + 1, 1}, ej[4] = {1, nfp, N + 1, N - nfp + 1};
+      for (int f = 0; f < 4; f++)
+        if (iface2fp[nfp - 1 + N * f] != ei[f] || jface2fp[nfp - 1 + N * f] != ej[f])
+          return set_err(CHORUS_EINVAL, "iface2fp/jface2fp differ from face2fpconnec");
+    }
+  ChorusCtx* c = new ChorusCtx();
+  c->device = device;
+  c->dims = *dims;
+  c->p = *params;
+  c->D = dispatch_for(N);
+  for (int w = 0; w < 4; w++) c->L[w] = default_launch(N, w);
+  auto fail = [&](int code) {
+    if (c->arena) cudaFree(c->arena);
+    if (c->st) cudaStreamDestroy(c->st);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    delete c;
+    return code;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return fail(set_err(CHORUS_ECUDA, "cudaSetDevice(%d) failed", device));
+
+  // ---- faces: interior + periodic pairs are two-sided, FREE faces one-sided
+  const int NI = dims->NINTER, NP = dims->NPAIR, NB = dims->NFREE;
+  std::vector<int4> f2;
+  std::vector<int2> f1;
+  f2.reserve(NI + NP);
+  auto cell_ok = [&](int ic) { return ic >= 1 && ic <= NC; };
+  auto lf_ok = [&](int l) { return l >= 1 && l <= 4; };
+  for (int i = 0; i < NI; i++) {
+    const int f = IBFINTER[i] - 1;
+    if (f < 0 || f >= NF) return fail(set_err(CHORUS_EMESH, "IBFINTER(%d)=%d out of range", i + 1, f + 1));
+    const int cl = IF2C[f], cr = IF2C[f + NF], ll = IF2C[f + 2 * NF], lr = IF2C[f + 3 * NF];
+    if (!cell_ok(cl) || !cell_ok(cr) || !lf_ok(ll) || !lf_ok(lr))
+      return fail(set_err(CHORUS_EMESH, "IF2C row %d inconsistent", f + 1));
+    f2.push_back(make_int4(cl - 1, ll, cr - 1, lr));
+  }
+  for (int i = 0; i < NP; i++) {
+    const int k1 = CYC2FPAIR[i] - 1, k2 = CYC2FPAIR[i + NP] - 1;
+    if (k1 < 0 || k1 >= NF || k2 < 0 || k2 >= NF) return fail(set_err(CHORUS_EMESH, "CYC2FPAIR(%d) out of range", i + 1));
+    const int cl = IF2C[k1], cr = IF2C[k2], ll = IF2C[k1 + 2 * NF], lr = IF2C[k2 + 2 * NF];
+    if (!cell_ok(cl) || !cell_ok(cr) || !lf_ok(ll) || !lf_ok(lr))
+      return fail(set_err(CHORUS_EMESH, "periodic pair %d inconsistent", i + 1));
+    f2.push_back(make_int4(cl - 1, ll, cr - 1, lr));
+  }
+  for (int i = 0; i < NB; i++) {
+    const int f = IBFREE[i] - 1;
+    if (f < 0 || f >= NF) return fail(set_err(CHORUS_EMESH, "IBFREE(%d) out of range", i + 1));
+    const int cl = IF2C[f], ll = IF2C[f + 2 * NF];
+    if (!cell_ok(cl) || !lf_ok(ll)) return fail(set_err(CHORUS_EMESH, "IF2C row %d inconsistent", f + 1));
+    f1.push_back(make_int2(cl - 1, ll));
+  }
+  c->nface2 = (int)f2.size();
+  c->nface1 = (int)f1.size();
+
+  // ---- derived geometry
+  const int NS = N * N, NF1 = (N + 1) * N, NFP = 2 * NF1, NG = 4 * (N + 1);
+  auto S1at = [&](int a, int b, int ifp, int jfp, int ic) {
+    return S1[a + 2 * (b + 2 * (ifp + (N + 1) * (jfp + (size_t)N * ic)))];
+  };
+  auto S2at = [&](int a, int b, int ifp, int jfp, int ic) {
+    return S2[a + 2 * (b + 2 * (ifp + N * (jfp + (size_t)(N + 1) * ic)))];
+  };
+  auto Jat = [&](int is, int js, int ic) { return Jac[is + N * (js + (size_t)N * ic)]; };
+  std::vector<double> met((size_t)NC * NFP * 2), gco((size_t)NC * NS * NG), invJ((size_t)NC * NS);
+  for (int ic = 0; ic < NC; ic++) {
+    for (int jfp = 0; jfp < N; jfp++)
+      for (int ifp = 0; ifp <= N; ifp++) {
+        size_t g = ((size_t)ic * NFP + jfp * (N + 1) + ifp) * 2;
+        met[g] = S1at(0, 0, ifp, jfp, ic);
+        met[g + 1] = S1at(0, 1, ifp, jfp, ic);
+      }
+    for (int jfp = 0; jfp <= N; jfp++)
+      for (int ifp = 0; ifp < N; ifp++) {
+        size_t g = ((size_t)ic * NFP + NF1 + jfp * N + ifp) * 2;
+        met[g] = S2at(1, 0, ifp, jfp, ic);
+        met[g + 1] = S2at(1, 1, ifp, jfp, ic);
+      }
+    for (int js = 0; js < N; js++)
+      for (int is = 0; is < N; is++) {
+        const double J = Jat(is, js, ic);
+        if (!(J > 0.0)) {
+          int code = set_err(CHORUS_EMESH, "Jacobian %g <= 0 in cell %d", J, ic + 1);
+          return fail(code);
+        }
+        invJ[(size_t)ic * NS + js * N + is] = 1.0 / J;
+        double* w = &gco[((size_t)ic * NS + js * N + is) * NG];
+        for (int r = 0; r <= N; r++) {
+          w[r] = Mmat[r + (N + 1) * is] * S1at(0, 0, r, js, ic) / J;
+          w[(N + 1) + r] = Mmat[r + (N + 1) * js] * S2at(1, 0, is, r, ic) / J;
+          w[2 * (N + 1) + r] = Mmat[r + (N + 1) * is] * S1at(0, 1, r, js, ic) / J;
+          w[3 * (N + 1) + r] = Mmat[r + (N + 1) * js] * S2at(1, 1, is, r, ic) / J;
+        }
+      }
+  }
+  // face normals from the left cell, getrusanov.f90:12-17 and interfaceflux_all.f90:46-76
+  auto normal = [&](int cl, int lf, int nfp, double& n1, double& n2) {
+    int ifp, jfp;
+    switch (lf) {
+      case 1: ifp = nfp; jfp = 0; n1 = S2at(1, 0, ifp, jfp, cl); n2 = S2at(1, 1, ifp, jfp, cl); break;
+      case 2: ifp = N; jfp = nfp; n1 = S1at(0, 0, ifp, jfp, cl); n2 = S1at(0, 1, ifp, jfp, cl); break;
+      case 3: ifp = N - 1 - nfp; jfp = N; n1 = S2at(1, 0, ifp, jfp, cl); n2 = S2at(1, 1, ifp, jfp, cl); break;
+      default: ifp = 0; jfp = N - 1 - nfp; n1 = S1at(0, 0, ifp, jfp, cl); n2 = S1at(0, 1, ifp, jfp, cl); break;
+    }
+  };
+  std::vector<FaceNorm> fn2((size_t)c->nface2 * N), fn1((size_t)c->nface1 * N);
+  auto fill = [&](int cl, int ll, int lr, int nfp, FaceNorm& o) {
+    double n1, n2;
+    normal(cl, ll, nfp, n1, n2);
+    const int sign_l = (ll == 1 || ll == 4) ? -1 : 1;
+    const int sign_r = (lr == 2 || lr == 3) ? -1 : 1;
+    const double mag = std::sqrt(n1 * n1 + n2 * n2);
+    o.ux = n1 / mag * sign_l;
+    o.uy = n2 / mag * sign_l;
+    o.msl = mag * sign_l;
+    o.ss = (double)(sign_l * sign_r);
+  };
+  for (int f = 0; f < c->nface2; f++)
+    for (int nfp = 0; nfp < N; nfp++) fill(f2[f].x, f2[f].y, f2[f].w, nfp, fn2[(size_t)f * N + nfp]);
+  for (int f = 0; f < c->nface1; f++)
+    for (int nfp = 0; nfp < N; nfp++) fill(f1[f].x, f1[f].y, 1, nfp, fn1[(size_t)f * N + nfp]);
+
+  // ---- device arena
+  const size_t nq = (size_t)NC * NS * 9, nfp = (size_t)NC * NFP;
+  ArenaPlan P;
+  size_t oQ = P.take<double>(nq), oQk0 = P.take<double>(nq), oQka = P.take<double>(nq);
+  const bool five = params->k_stage == 5;
+  size_t oQr2 = five ? P.take<double>(nq) : 0, oQr3 = five ? P.take<double>(nq) : 0, oR0 = five ? P.take<double>(nq) : 0;
+  size_t oRes = P.take<double>(nq), oQvf = P.take<double>(nfp * 9), oFc = P.take<double>(nfp * 8),
+         oAzf = P.take<double>(nfp), onQs = P.take<double>((size_t)NC * NS * 18), onQvf = P.take<double>(nfp * 18),
+         onAs = P.take<double>((size_t)NC * NS * 2), omet = P.take<double>(nfp * 2),
+         ogco = P.take<double>((size_t)NC * NS * NG), oinvJ = P.take<double>((size_t)NC * NS),
+         oSe = P.take<double>(NC), omuf = P.take<double>((size_t)NC * 4), odiag = P.take<double>((size_t)NC * 2),
+         of2 = P.take<int4>(f2.size() + 1), of1 = P.take<int2>(f1.size() + 1),
+         ofn2 = P.take<FaceNorm>(fn2.size() + 1), ofn1 = P.take<FaceNorm>(fn1.size() + 1),
+         oeig = P.take<unsigned long long>(4), oerr = P.take<unsigned int>(4), ored = P.take<double>(8);
+  c->arena_bytes = P.off;
+  cudaError_t e = cudaMalloc(&c->arena, P.off);
+  if (e != cudaSuccess)
+    return fail(set_err(CHORUS_ENOMEM, "cudaMalloc(%zu bytes) failed: %s", P.off, cudaGetErrorString(e)));
+  char* A = (char*)c->arena;
+  SolveDev& s = c->sd;
+  s.N = N;
+  s.NC = NC;
+  s.nface2 = c->nface2;
+  s.nface1 = c->nface1;
+  s.artiv = params->ARTIV == 1;
+  s.gam = params->gam;
+  s.mu = params->mu;
+  s.eta0 = params->eta0;
+  s.B0x = params->B0x;
+  s.B0y = params->B0y;
+  s.hmsh = std::sqrt(params->DXCYCL * params->DYCYCL / (double)params->NCELLGLOB);
+  s.Q = (double*)(A + oQ);
+  s.Qk0 = (double*)(A + oQk0);
+  s.Qka = (double*)(A + oQka);
+  s.Qr2 = five ? (double*)(A + oQr2) : nullptr;
+  s.Qr3 = five ? (double*)(A + oQr3) : nullptr;
+  s.R0 = five ? (double*)(A + oR0) : nullptr;
+  s.resid = (double*)(A + oRes);
+  s.Qvf = (double*)(A + oQvf);
+  s.Fc = (double*)(A + oFc);
+  s.Azf = (double*)(A + oAzf);
+  s.nQs = (double*)(A + onQs);
+  s.nQvf = (double*)(A + onQvf);
+  s.nAs = (double*)(A + onAs);
+  s.met = (const double*)(A + omet);
+  s.gco = (const double*)(A + ogco);
+  s.invJ = (const double*)(A + oinvJ);
+  s.Se = (double*)(A + oSe);
+  s.muf = (double*)(A + omuf);
+  s.diag = (double*)(A + odiag);
+  s.face2 = (const int4*)(A + of2);
+  s.face1 = (const int2*)(A + of1);
+  s.fn2 = (const FaceNorm*)(A + ofn2);
+  s.fn1 = (const FaceNorm*)(A + ofn1);
+  s.eig = (unsigned long long*)(A + oeig);
+  s.err = (unsigned int*)(A + oerr);
+  c->red = (double*)(A + ored);
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(set_err(CHORUS_ECUDA, "stream creation failed"));
+  if (cudaMallocHost(&c->h_pinned, 64 * sizeof(double)) != cudaSuccess)
+    return fail(set_err(CHORUS_ECUDA, "pinned allocation failed"));
+  e = cudaMemsetAsync(c->arena, 0, P.off, c->st);
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->st);
+  };
+  up((void*)s.met, met.data(), met.size() * sizeof(double));
+  up((void*)s.gco, gco.data(), gco.size() * sizeof(double));
+  up((void*)s.invJ, invJ.data(), invJ.size() * sizeof(double));
+  up((void*)s.face2, f2.data(), f2.size() * sizeof(int4));
+  up((void*)s.face1, f1.data(), f1.size() * sizeof(int2));
+  up((void*)s.fn2, fn2.data(), fn2.size() * sizeof(FaceNorm));
+  up((void*)s.fn1, fn1.data(), fn1.size() * sizeof(FaceNorm));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return fail(set_err(CHORUS_ECUDA, "upload failed: %s", cudaGetErrorString(e)));
+  int rc = ensure_ops(device, N, Lmat, Mmat, Xs, Xf);
+  if (rc) return fail(rc);
+  *out = c;
+  return CHORUS_OK;
+}
+
+int chorus_gpu_free(ChorusCtx* c) {
+  if (!c) return CHORUS_OK;
+  cudaSetDevice(c->device);
+  if (c->g_step) cudaGraphExecDestroy(c->g_step);
+  if (c->g_diag) cudaGraphExecDestroy(c->g_diag);
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->arena) cudaFree(c->arena);
+  if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return CHORUS_OK;
+}
+
+static void drop_graphs(ChorusCtx* c) {
+  if (c->g_step) cudaGraphExecDestroy(c->g_step);
+  if (c->g_diag) cudaGraphExecDestroy(c->g_diag);
+  c->g_step = c->g_diag = nullptr;
+}
+
+int chorus_gpu_set_params(ChorusCtx* c, const ChorusParams* p) {
+  if (!c || !p) return set_err(CHORUS_EINVAL, "null argument");
+  if (p->k_stage != c->p.k_stage) return set_err(CHORUS_EINVAL, "k_stage is fixed at bind time");
+  c->p.dt = p->dt;
+  c->p.mu = p->mu;
+  c->p.eta0 = p->eta0;
+  c->p.ARTIV = p->ARTIV;
+  c->sd.mu = p->mu;
+  c->sd.eta0 = p->eta0;
+  c->sd.artiv = p->ARTIV == 1;
+  drop_graphs(c);
+  return CHORUS_OK;
+}
+
+int chorus_gpu_upload_state(ChorusCtx* c, const double* Q) {
+  if (!c || !Q) return set_err(CHORUS_EINVAL, "null argument");
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  const size_t n = (size_t)c->dims.NCELL * c->dims.N * c->dims.N * 9;
+  CK(cudaMemcpyAsync(c->sd.Q, Q, n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return CHORUS_OK;
+}
+
+int chorus_gpu_download_state(ChorusCtx* c, double* Q) {
+  if (!c || !Q) return set_err(CHORUS_EINVAL, "null argument");
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  const size_t n = (size_t)c->dims.NCELL * c->dims.N * c->dims.N * 9;
+  CK(cudaMemcpyAsync(Q, c->sd.Q, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return CHORUS_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// stage sequences
+// ---------------------------------------------------------------------------
+namespace {
+
+void enqueue_stage(ChorusCtx* c, const RKStage& rk) {
+  const SolveDev& s = c->sd;
+  cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st);
+  c->D->e1(s, c->L[0], c->st);
+  c->D->f1(s, c->st);
+  c->D->e2(s, c->L[1], c->st);
+  c->D->f2(s, c->st);
+  c->D->e3(s, rk, c->L[2], c->st);
+}
+
+void enqueue_ct(ChorusCtx* c) {
+  c->D->ct(c->sd, c->L[3], c->st, 0);
+  c->D->ct(c->sd, c->L[3], c->st, 1);
+  c->D->ct(c->sd, c->L[3], c->st, 2);
+}
+
+RKStage rk_blank() {
+  RKStage r;
+  std::memset(&r, 0, sizeof r);
+  return r;
+}
+
+// the five stages of RK_S5P3 (iterations.f90:162-217) or FiveStageRk (:92-160);
+// `diag` marks the last stage to accumulate the residual norm
+void enqueue_rk(ChorusCtx* c, bool diag) {
+  const SolveDev& s = c->sd;
+  const double dt = c->p.dt;
+  RKStage r[5];
+  for (auto& x : r) x = rk_blank();
+  if (c->p.k_stage == 5) {
+    const double a11 = 0.39175222700392, a21 = 0.44437049406734, a22 = 0.55562950593266, a23 = 0.36841059262959,
+                 a31 = 0.6201018513854, a32 = 0.3798981486146, a33 = 0.25189177424738, a41 = 0.17807995410773,
+                 a42 = 0.82192004589227, a43 = 0.54497475021237, a51 = 0.00683325884039, a52 = 0.51723167208978,
+                 a53 = 0.12759831133288, a54 = 0.34833675773694, a55 = 0.08460416338212, a56 = 0.22600748319395;
+    r[0].cQ = 1.0; r[0].cR = dt * a11; r[0].save_old = s.Qk0;
+    r[1].nsrc = 1; r[1].src[0] = s.Qk0; r[1].c[0] = a21; r[1].cQ = a22; r[1].cR = a23 * dt; r[1].save_new = s.Qr2;
+    r[2].nsrc = 1; r[2].src[0] = s.Qk0; r[2].c[0] = a31; r[2].cQ = a32; r[2].cR = a33 * dt; r[2].save_new = s.Qr3;
+    r[3].nsrc = 1; r[3].src[0] = s.Qk0; r[3].c[0] = a41; r[3].cQ = a42; r[3].cR = a43 * dt; r[3].save_R = s.R0;
+    r[4].nsrc = 3; r[4].src[0] = s.Qk0; r[4].src[1] = s.Qr2; r[4].src[2] = s.Qr3;
+    r[4].c[0] = a51; r[4].c[1] = a52; r[4].c[2] = a53; r[4].cQ = a54; r[4].cR = a56 * dt;
+    r[4].R0 = s.R0; r[4].cR0 = a55 * dt;
+  } else {
+    const double a30 = 0.355909775063327, a32 = 0.644090224936674, a40 = 0.367933791638137,
+                 a43 = 0.632066208361863, a52 = 0.237593836598569, a54 = 0.762406163401431,
+                 b10 = 0.377268915331368, b21 = 0.377268915331368, b32 = 0.242995220537396,
+                 b43 = 0.238458932846290, b54 = 0.287632146308408;
+    r[0].cQ = 1.0; r[0].cR = b10 * dt; r[0].save_old = s.Qk0;
+    r[1].cQ = 1.0; r[1].cR = b21 * dt; r[1].save_new = s.Qka;
+    r[2].nsrc = 1; r[2].src[0] = s.Qk0; r[2].c[0] = a30; r[2].cQ = a32; r[2].cR = b32 * dt;
+    r[3].nsrc = 1; r[3].src[0] = s.Qk0; r[3].c[0] = a40; r[3].cQ = a43; r[3].cR = b43 * dt;
+    r[4].nsrc = 1; r[4].src[0] = s.Qka; r[4].c[0] = a52; r[4].cQ = a54; r[4].cR = b54 * dt;
+  }
+  r[4].diag = diag ? 1 : 0;
+  r[4].write_resid = 1;  // the last stage's residual stays available like the reference's resid
+  for (int k = 0; k < 5; k++) enqueue_stage(c, r[k]);
+}
+
+__global__ void k_store_record(const double* red2, const unsigned long long* eig, double* rec) {
+  rec[0] = red2[0];
+  rec[1] = red2[1];
+  rec[2] = __longlong_as_double((long long)eig[0]);
+}
+
+// diagnostic of iterations.f90:35-76 on the CT-corrected state
+void enqueue_diag(ChorusCtx* c) {
+  SolveDev s = c->sd;
+  s.eig = c->sd.eig + 1;  // keep the last stage's wave speed for the record
+  c->D->e1ns(s, c->L[0], c->st);
+  c->D->f1(s, c->st);
+  c->D->nqsp(s, 5, 6, c->st);
+  c->D->divb(s, c->st);
+  launch_reduce_diag(s.diag, s.NC, c->red, c->st);
+  k_store_record<<<1, 1, 0, c->st>>>(c->red, c->sd.eig, c->red + 4);
+}
+
+int build_graphs(ChorusCtx* c) {
+  drop_graphs(c);
+  for (int which = 0; which < 2; which++) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    enqueue_rk(c, which == 1);
+    enqueue_ct(c);
+    if (which == 1) enqueue_diag(c);
+    CK(cudaStreamEndCapture(c->st, &g));
+    cudaGraphExec_t ex;
+    cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    (which ? c->g_diag : c->g_step) = ex;
+  }
+  c->graph_dt = c->p.dt;
+  c->graph_k = c->p.k_stage;
+  return CHORUS_OK;
+}
+
+int check_err_flag(ChorusCtx* c) {
+  unsigned int h = 0;
+  CK(cudaMemcpyAsync(&h, c->sd.err, sizeof h, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (h) return set_err(CHORUS_ESTATE, "kernels flagged a non-finite wave speed (state is not physical)");
+  return CHORUS_OK;
+}
+
+void advance_ctime(int k_stage, double dt, double* ctime) {
+  if (!ctime) return;
+  // ctime bookkeeping of RK_S5P3 / FiveStageRk: the step ends at ctime0 + dt
+  (void)k_stage;
+  *ctime = *ctime + dt;
+}
+
+}  // namespace
+
+extern "C" {
+
+int compresid_gpu(ChorusCtx* c) {
+  if (!c) return set_err(CHORUS_EINVAL, "null context");
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  RKStage r = rk_blank();
+  r.write_resid = 1;
+  enqueue_stage(c, r);
+  CK(cudaGetLastError());
+  return check_err_flag(c);
+}
+
+int comp_inviscid_flux_gpu(ChorusCtx* c) {
+  if (!c) return set_err(CHORUS_EINVAL, "null context");
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  c->D->e1ns(c->sd, c->L[0], c->st);
+  c->D->f1(c->sd, c->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  return CHORUS_OK;
+}
+
+int nablaqsp_gpu(ChorusCtx* c, const int32_t* v_sta, const int32_t* v_end) {
+  if (!c || !v_sta || !v_end) return set_err(CHORUS_EINVAL, "null argument");
+  if (*v_sta < 1 || *v_end > 9 || *v_sta > *v_end) return set_err(CHORUS_EINVAL, "variable range %d..%d", *v_sta, *v_end);
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  c->D->nqsp(c->sd, *v_sta - 1, *v_end - 1, c->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  return CHORUS_OK;
+}
+
+int correct_b_via_curl_az_gpu(ChorusCtx* c) {
+  if (!c) return set_err(CHORUS_EINVAL, "null context");
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  enqueue_ct(c);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  return CHORUS_OK;
+}
+
+static int one_step(ChorusCtx* c, double* ctime, int k_stage) {
+  if (!c) return set_err(CHORUS_EINVAL, "null context");
+  if (c->p.k_stage != k_stage) return set_err(CHORUS_EINVAL, "context was bound with k_stage=%d", c->p.k_stage);
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  enqueue_rk(c, false);
+  CK(cudaGetLastError());
+  advance_ctime(k_stage, c->p.dt, ctime);
+  return check_err_flag(c);
+}
+
+int rk_s5p3_gpu(ChorusCtx* c, double* ctime) { return one_step(c, ctime, 3); }
+int fivestagerk_gpu(ChorusCtx* c, double* ctime) { return one_step(c, ctime, 5); }
+
+int iterations_gpu(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime, ChorusDiag* diag, int32_t max_diag,
+                   int32_t* n_diag) {
+  if (!c || !iter || nsteps < 0) return set_err(CHORUS_EINVAL, "bad argument");
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  if (!c->g_step || c->graph_dt != c->p.dt || c->graph_k != c->p.k_stage) {
+    int rc = build_graphs(c);
+    if (rc) return rc;
+  }
+  int nd = 0;
+  std::vector<int> diag_iters;
+  std::vector<double> diag_times;
+  const int N = c->dims.N;
+  double* recs = c->h_pinned;  // up to 16 records of 3 doubles per sync window
+  int pending = 0;
+  auto flush = [&]() -> int {
+    if (!pending) return CHORUS_OK;
+    CK(cudaStreamSynchronize(c->st));
+    for (int i = 0; i < pending; i++) {
+      if (diag && nd < max_diag) {
+        ChorusDiag& d = diag[nd];
+        std::memset(&d, 0, sizeof d);
+        d.iter = diag_iters[i];
+        d.ctime = diag_times[i];
+        const double nglob = (double)c->p.NCELLGLOB;
+        d.residglob = std::sqrt(recs[3 * i] / (double)(c->p.NCELLGLOB * N * N * 5));
+        d.divBglob = std::sqrt(recs[3 * i + 1] / (nglob * N * N));
+        d.eigvmax_g = recs[3 * i + 2];
+        d.epsilon0 = d.eigvmax_g * c->sd.hmsh / (N - 1) * 1.0;
+      }
+      nd++;
+    }
+    pending = 0;
+    diag_iters.clear();
+    diag_times.clear();
+    return CHORUS_OK;
+  };
+  for (int s = 0; s < nsteps; s++) {
+    *iter = *iter + 1;
+    const bool d = (*iter % 10) == 1;
+    CK(cudaGraphLaunch(d ? c->g_diag : c->g_step, c->st));
+    if (ctime) *ctime = *ctime + c->p.dt;
+    if (d) {
+      CK(cudaMemcpyAsync(recs + 3 * pending, c->red + 4, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+      diag_iters.push_back(*iter);
+      diag_times.push_back(ctime ? *ctime : 0.0);
+      pending++;
+      if (pending == 16) {
+        int rc = flush();
+        if (rc) return rc;
+      }
+    }
+  }
+  int rc = flush();
+  if (rc) return rc;
+  if (n_diag) *n_diag = nd;
+  return check_err_flag(c);
+}
+
+int chorus_gpu_get_eigvmax(ChorusCtx* c, double* eigvmax_g, double* epsilon0) {
+  if (!c) return set_err(CHORUS_EINVAL, "null context");
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  unsigned long long b = 0;
+  CK(cudaMemcpyAsync(&b, c->sd.eig, sizeof b, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  double ev;
+  std::memcpy(&ev, &b, sizeof ev);
+  if (eigvmax_g) *eigvmax_g = ev;
+  if (epsilon0) *epsilon0 = ev * c->sd.hmsh / (c->dims.N - 1) * 1.0;
+  return CHORUS_OK;
+}
+
+int chorus_gpu_download_array(ChorusCtx* c, const char* name, double* out, int64_t count) {
+  if (!c || !name || !out) return set_err(CHORUS_EINVAL, "null argument");
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  const int N = c->dims.N, NC = c->dims.NCELL, NS = N * N, NF1 = (N + 1) * N, NFP = 2 * NF1;
+  const SolveDev& s = c->sd;
+  std::string n(name);
+  auto pull = [&](const double* src, size_t cnt, std::vector<double>& h) -> int {
+    h.resize(cnt);
+    CK(cudaMemcpyAsync(h.data(), src, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return CHORUS_OK;
+  };
+  std::vector<double> h;
+  // same layout as the reference
+  struct Same { const char* nm; const double* p; size_t cnt; } same[] = {
+      {"resid", s.resid, (size_t)NC * NS * 9}, {"nablaQs", s.nQs, (size_t)NC * NS * 18},
+      {"nablaAs", s.nAs, (size_t)NC * NS * 2}, {"Q", s.Q, (size_t)NC * NS * 9}, {"SM_IND1", s.Se, (size_t)NC}};
+  for (auto& x : same)
+    if (n == x.nm) {
+      if ((size_t)count != x.cnt) return set_err(CHORUS_EINVAL, "%s has %zu elements, not %lld", name, x.cnt, (long long)count);
+      CK(cudaMemcpyAsync(out, x.p, x.cnt * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      return CHORUS_OK;
+    }
+  // per-cell flux-point blocks split into the family-1 / family-2 arrays
+  struct Split { const char* nm; const double* p; int w; int fam; } split[] = {
+      {"Qvfi", s.Qvf, 9, 0}, {"Qvfj", s.Qvf, 9, 1}, {"F1", s.Fc, 8, 0}, {"G2", s.Fc, 8, 1},
+      {"Azfi", s.Azf, 1, 0}, {"Azfj", s.Azf, 1, 1}, {"nablaQvfi", s.nQvf, 18, 0}, {"nablaQvfj", s.nQvf, 18, 1}};
+  for (auto& x : split)
+    if (n == x.nm) {
+      const size_t per = (size_t)NF1 * x.w;
+      if ((size_t)count != per * NC) return set_err(CHORUS_EINVAL, "%s has %zu elements", name, per * NC);
+      int rc = pull(x.p, (size_t)NC * NFP * x.w, h);
+      if (rc) return rc;
+      for (int e = 0; e < NC; e++)
+        std::memcpy(out + per * e, h.data() + ((size_t)e * NFP + (size_t)x.fam * NF1) * x.w, per * sizeof(double));
+      return CHORUS_OK;
+    }
+  if (n == "muAVfi" || n == "muAVfj") {
+    if ((size_t)count != (size_t)NC * 18) return set_err(CHORUS_EINVAL, "%s has %d elements", name, NC * 18);
+    int rc = pull(s.muf, (size_t)NC * 4, h);
+    if (rc) return rc;
+    std::memset(out, 0, sizeof(double) * NC * 18);
+    const bool fi = n == "muAVfi";
+    for (int e = 0; e < NC; e++) {
+      out[0 + 9 * (0 + 2 * e)] = fi ? h[4 * e + 3] : h[4 * e + 0];
+      out[0 + 9 * (1 + 2 * e)] = fi ? h[4 * e + 1] : h[4 * e + 2];
+    }
+    return CHORUS_OK;
+  }
+  return set_err(CHORUS_EINVAL, "unknown array %s", name);
+}
+
+// ---------------------------------------------------------------------------
+// point functions over n points (host arrays)
+// ---------------------------------------------------------------------------
+}  // extern "C"
+template <typename T>
+static int dev_copy(T** d, const T* h, size_t n, cudaStream_t st) {
+  CK(cudaMalloc(d, std::max<size_t>(n, 1) * sizeof(T)));
+  if (h) CK(cudaMemcpyAsync(*d, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
+  return CHORUS_OK;
+}
+extern "C" {
+
+int getrusanovflux_gpu(int32_t n, double gam, const double* Qfl, const double* Qfr, double* Fnl, double* Fnr,
+                       double* Az, const double* normf, const int32_t* sign_l, const int32_t* sign_r, double* eigv) {
+  if (n < 0 || (n > 0 && (!Qfl || !Qfr || !Fnl || !Fnr || !Az || !normf || !sign_l || !sign_r || !eigv)))
+    return set_err(CHORUS_EINVAL, "bad argument");
+  if (n == 0) return CHORUS_OK;
+  double *a, *b, *fl, *fr, *az, *nf, *ev;
+  int *sl, *sr;
+  cudaStream_t st = 0;
+  int rc = dev_copy(&a, Qfl, 9 * (size_t)n, st) || dev_copy(&b, Qfr, 9 * (size_t)n, st) ||
+           dev_copy<double>(&fl, nullptr, 8 * (size_t)n, st) || dev_copy<double>(&fr, nullptr, 8 * (size_t)n, st) ||
+           dev_copy<double>(&az, nullptr, n, st) || dev_copy(&nf, normf, 2 * (size_t)n, st) ||
+           dev_copy<double>(&ev, nullptr, n, st) || dev_copy(&sl, (const int*)sign_l, n, st) ||
+           dev_copy(&sr, (const int*)sign_r, n, st);
+  if (rc) return CHORUS_ECUDA;
+  launch_point_rusanov(n, gam, a, b, fl, fr, az, nf, sl, sr, ev, st);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(Fnl, fl, 8 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(Fnr, fr, 8 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(Az, az, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(eigv, ev, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  void* ptrs[] = {a, b, fl, fr, az, nf, ev, sl, sr};
+  for (void* p : ptrs) cudaFree(p);
+  if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "getrusanovflux_gpu: %s", cudaGetErrorString(e));
+  return CHORUS_OK;
+}
+
+int getifluxvectors_gpu(int32_t n, double gam, const double* Qi, double* Fi, double* Gi) {
+  if (n < 0 || (n > 0 && (!Qi || !Fi || !Gi))) return set_err(CHORUS_EINVAL, "bad argument");
+  if (n == 0) return CHORUS_OK;
+  double *q, *f, *g;
+  if (dev_copy(&q, Qi, 8 * (size_t)n, 0) || dev_copy<double>(&f, nullptr, 8 * (size_t)n, 0) ||
+      dev_copy<double>(&g, nullptr, 8 * (size_t)n, 0))
+    return CHORUS_ECUDA;
+  launch_point_iflux(n, gam, q, f, g, 0);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(Fi, f, 8 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(Gi, g, 8 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(q); cudaFree(f); cudaFree(g);
+  if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "getifluxvectors_gpu: %s", cudaGetErrorString(e));
+  return CHORUS_OK;
+}
+
+int getvfluxvectors_gpu(int32_t n, double gam, double mu, double eta0, const double* Qv, const double* nablaQ,
+                        double* Fv, double* Gv) {
+  if (n < 0 || (n > 0 && (!Qv || !nablaQ || !Fv || !Gv))) return set_err(CHORUS_EINVAL, "bad argument");
+  if (n == 0) return CHORUS_OK;
+  double *q, *g, *f, *h;
+  if (dev_copy(&q, Qv, 9 * (size_t)n, 0) || dev_copy(&g, nablaQ, 18 * (size_t)n, 0) ||
+      dev_copy<double>(&f, nullptr, 9 * (size_t)n, 0) || dev_copy<double>(&h, nullptr, 9 * (size_t)n, 0))
+    return CHORUS_ECUDA;
+  launch_point_vflux(n, gam, mu, eta0, q, g, f, h, 0);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(Fv, f, 9 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(Gv, h, 9 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(q); cudaFree(g); cudaFree(f); cudaFree(h);
+  if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "getvfluxvectors_gpu: %s", cudaGetErrorString(e));
+  return CHORUS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host-side setup
+// ---------------------------------------------------------------------------
+struct ChorusMesh {
+  Mesh m;
+};
+
+int chorus_mesh_load(const char* dir, ChorusMesh** out) {
+  if (!dir || !out) return set_err(CHORUS_EINVAL, "null argument");
+  *out = nullptr;
+  ChorusMesh* mh = new ChorusMesh();
+  std::string err;
+  int rc = mesh_load(dir, mh->m, err);
+  if (rc) {
+    delete mh;
+    return set_err(rc, "%s", err.c_str());
+  }
+  *out = mh;
+  return CHORUS_OK;
+}
+
+int chorus_mesh_free(ChorusMesh* mh) {
+  delete mh;
+  return CHORUS_OK;
+}
+
+int chorus_mesh_info(const ChorusMesh* mh, ChorusDims* dims, ChorusParams* params, int32_t* maxiter, int32_t* problem) {
+  if (!mh) return set_err(CHORUS_EINVAL, "null mesh");
+  const Mesh& m = mh->m;
+  if (dims) {
+    dims->N = m.N;
+    dims->NCELL = m.NCELL;
+    dims->NFACE = m.NFACE;
+    dims->NINTER = (int)m.IBFINTER.size();
+    dims->NFREE = (int)m.IBFREE.size();
+    dims->NPAIR = m.NPAIR;
+  }
+  if (params) *params = m.params;
+  if (maxiter) *maxiter = m.maxiter;
+  if (problem) *problem = m.problem;
+  return CHORUS_OK;
+}
+
+const int32_t* chorus_mesh_iarray(const ChorusMesh* mh, const char* name, int64_t* count) {
+  if (!mh || !name) return nullptr;
+  const Mesh& m = mh->m;
+  struct { const char* n; const std::vector<int32_t>* v; } t[] = {
+      {"IF2C", &m.IF2C}, {"IC2F", &m.IC2F}, {"IF2V", &m.IF2V}, {"IVCELL", &m.IVCELL}, {"IBFINTER", &m.IBFINTER},
+      {"IBFREE", &m.IBFREE}, {"IBFCYC", &m.IBFCYC}, {"IBFCYCLOC", &m.IBFCYCLOC}, {"CYC2FPAIR", &m.CYC2FPAIR},
+      {"iface2fp", &m.iface2fp}, {"jface2fp", &m.jface2fp}};
+  static const int32_t empty = 0;
+  for (auto& x : t)
+    if (!std::strcmp(name, x.n)) {
+      if (count) *count = (int64_t)x.v->size();
+      return x.v->empty() ? &empty : x.v->data();
+    }
+  if (count) *count = 0;
+  return nullptr;
+}
+
+const double* chorus_mesh_darray(const ChorusMesh* mh, const char* name, int64_t* count) {
+  if (!mh || !name) return nullptr;
+  const Mesh& m = mh->m;
+  struct { const char* n; const std::vector<double>* v; } t[] = {
+      {"XV", &m.XV}, {"YV", &m.YV}, {"Xs", &m.Xs}, {"Xf", &m.Xf}, {"Lmat", &m.Lmat}, {"Mmat", &m.Mmat},
+      {"S1", &m.S1}, {"S2", &m.S2}, {"Jac", &m.Jac}, {"XXsolu", &m.XXsolu}};
+  static const double empty = 0.0;
+  for (auto& x : t)
+    if (!std::strcmp(name, x.n)) {
+      if (count) *count = (int64_t)x.v->size();
+      return x.v->empty() ? &empty : x.v->data();
+    }
+  if (count) *count = 0;
+  return nullptr;
+}
+
+int chorus_gpu_bind_mesh(const ChorusMesh* mh, int32_t device, ChorusCtx** ctx) {
+  if (!mh) return set_err(CHORUS_EINVAL, "null mesh");
+  const Mesh& m = mh->m;
+  ChorusDims d;
+  chorus_mesh_info(mh, &d, nullptr, nullptr, nullptr);
+  return chorus_gpu_bind(&d, m.IF2C.data(), m.IBFINTER.data(), m.IBFREE.data(), m.CYC2FPAIR.data(), m.iface2fp.data(),
+                         m.jface2fp.data(), m.Xs.data(), m.Xf.data(), m.Lmat.data(), m.Mmat.data(), m.S1.data(),
+                         m.S2.data(), m.Jac.data(), &m.params, device, ctx);
+}
+
+int chorus_initial_state(const ChorusMesh* mh, ChorusCtx* c, double* Qout) {
+  if (!mh || !c) return set_err(CHORUS_EINVAL, "null argument");
+  const Mesh& m = mh->m;
+  const int N = m.N, NC = m.NCELL;
+  if (c->dims.N != N || c->dims.NCELL != NC) return set_err(CHORUS_EINVAL, "mesh and context differ");
+  const size_t np = (size_t)NC * N * N;
+  std::vector<double> Q(np * 9);
+  for (size_t p = 0; p < np; p++) initial_point(m.problem, m.params.gam, m.XXsolu[2 * p], m.XXsolu[2 * p + 1], nullptr, &Q[9 * p]);
+  int rc = chorus_gpu_upload_state(c, Q.data());
+  if (!rc) rc = correct_b_via_curl_az_gpu(c);
+  if (!rc) rc = chorus_gpu_download_state(c, Q.data());
+  if (rc) return rc;
+  for (size_t p = 0; p < np; p++) {
+    double B[3] = {Q[9 * p + 5], Q[9 * p + 6], Q[9 * p + 7]};
+    initial_point(m.problem, m.params.gam, m.XXsolu[2 * p], m.XXsolu[2 * p + 1], B, &Q[9 * p]);
+  }
+  rc = chorus_gpu_upload_state(c, Q.data());
+  if (rc) return rc;
+  if (Qout) std::memcpy(Qout, Q.data(), Q.size() * sizeof(double));
+  return CHORUS_OK;
+}
+
+int chorus_write_restart(ChorusCtx* c, const char* path, int32_t iter, double ctime) {
+  if (!c || !path) return set_err(CHORUS_EINVAL, "null argument");
+  const int N = c->dims.N, NC = c->dims.NCELL, nq = 9 * N * N;
+  std::vector<double> Q((size_t)NC * nq);
+  int rc = chorus_gpu_download_state(c, Q.data());
+  if (rc) return rc;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return set_err(CHORUS_EIO, "cannot open %s", path);
+  bool ok = std::fwrite(&iter, 4, 1, f) == 1 && std::fwrite(&ctime, 8, 1, f) == 1;
+  for (int e = 0; e < NC && ok; e++) {
+    int32_t g = e + 1;
+    ok = std::fwrite(&g, 4, 1, f) == 1 && std::fwrite(&Q[(size_t)e * nq], 8, nq, f) == (size_t)nq;
+  }
+  std::fclose(f);
+  return ok ? CHORUS_OK : set_err(CHORUS_EIO, "short write to %s", path);
+}
+
+int chorus_read_restart(ChorusCtx* c, const char* path, int32_t* iter, double* ctime) {
+  if (!c || !path) return set_err(CHORUS_EINVAL, "null argument");
+  const int N = c->dims.N, NC = c->dims.NCELL, nq = 9 * N * N;
+  std::vector<double> Q((size_t)NC * nq, 0.0);
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_err(CHORUS_EIO, "cannot open %s", path);
+  int32_t it = 0;
+  double t = 0;
+  bool ok = std::fread(&it, 4, 1, f) == 1 && std::fread(&t, 8, 1, f) == 1;
+  for (int e = 0; e < NC && ok; e++) {
+    int32_t g = 0;
+    ok = std::fread(&g, 4, 1, f) == 1 && g >= 1 && g <= NC;
+    if (ok) ok = std::fread(&Q[(size_t)(g - 1) * nq], 8, nq, f) == (size_t)nq;
+  }
+  std::fclose(f);
+  if (!ok) return set_err(CHORUS_EIO, "bad restart file %s", path);
+  if (iter) *iter = it;
+  if (ctime) *ctime = t;
+  return chorus_gpu_upload_state(c, Q.data());
+}
+
+}  // extern "C"

@@ -1,0 +1,129 @@
+// chorus_internal.h -- types shared by the host runtime and the CUDA kernels.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <cuda_runtime.h>
+#include <vector>
+
+#include "../../include/chorus_gpu.h"
+
+namespace chorus {
+
+constexpr int kMaxN = 8;   // kernels are instantiated for N = 2..kMaxN
+constexpr int kMinN = 2;
+
+// ---------------------------------------------------------------------------
+// Host-side mesh (what the reference's setup chain leaves in module setup2d)
+// ---------------------------------------------------------------------------
+struct Mesh {
+  int N = 0, NCELL = 0, NVERT = 0, NFACE = 0, NPAIR = 0;
+  int maxiter = 0, problem = 0, restart = 0;
+  ChorusParams params{};
+  std::vector<int32_t> IVCELL, IC2F, IF2C, IF2V, IBFINTER, IBFREE, IBFCYC, IBFCYCLOC, CYC2FPAIR;
+  std::vector<int32_t> iface2fp, jface2fp;
+  std::vector<double> XV, YV, Xs, Xf, Lmat, Mmat, S1, S2, Jac, XXsolu;
+};
+
+int mesh_load(const std::string& dir, Mesh& m, std::string& err);
+void setsandpoints(int np, double* xs, double* xf);
+double lagrange(const double* x, int n, int i, double xv);
+void compute_L_M(int N, const double* Xs, const double* Xf, double* L, double* M);
+void initial_point(int problem, double gam, double x, double y, const double* B, double* q);
+
+// ---------------------------------------------------------------------------
+// Device-side view of one solve.  Element-blocked layouts (e = cell, 0-based):
+//   Q, Qk0..   [e][js][is][9]              (the reference's Q(9,N,N,NC))
+//   resid      [e][js][is][9]
+//   Qvf        [e][fp][9]    fp = family-1 points (jfp*(N+1)+ifp), then family-2
+//                            points ((N+1)N + jfp*N+ifp): one block per cell
+//   Fc         [e][fp][8]    inviscid contravariant flux (F1 / G2)
+//   Azf        [e][fp]       A_z at the flux points (upwinded on faces)
+//   nQs        [e][js][is][2][9]
+//   nQvf       [e][fp][2][9]
+//   nAs        [e][js][is][2]
+//   met        [e][fp][2]    (S1(1,1),S1(1,2)) on family 1, (S2(2,1),S2(2,2)) on 2
+//   gco        [e][js][is][4][N+1] gradient weights Mmat*S/Jac (x-fam1, x-fam2,
+//                            y-fam1, y-fam2)
+//   invJ       [e][js][is]
+//   Se         [e]           AV sensor of variable 1 (log10)
+//   muf        [e][4]        face-averaged AV viscosity per local face 1..4
+// ---------------------------------------------------------------------------
+struct FaceNorm {  // per two-sided face point: unit normal, magnorm*sign_l, sign_l*sign_r
+  double ux, uy, msl, ss;
+};
+
+struct SolveDev {
+  int N, NC;
+  int nface2, nface1;           // two-sided faces (interior + periodic), FREE faces
+  int artiv;
+  int pad0;
+  double gam, mu, eta0, B0x, B0y, hmsh;
+  double* Q;
+  double* Qk0;
+  double* Qka;
+  double* Qr2;                  // extra registers for FiveStageRk (qj2, qj3, resid0)
+  double* Qr3;
+  double* R0;
+  double* resid;
+  double* Qvf;
+  double* Fc;
+  double* Azf;
+  double* nQs;
+  double* nQvf;
+  double* nAs;
+  const double* met;
+  const double* gco;
+  const double* invJ;
+  double* Se;
+  double* muf;
+  const int4* face2;            // (cL, lfL, cR, lfR): cells 0-based, local faces 1..4
+  const FaceNorm* fn2;          // [face][nfp]
+  const int2* face1;            // (c, lf)
+  const FaceNorm* fn1;          // [face][nfp] (ss unused)
+  unsigned long long* eig;      // bit pattern of the stage's max wave speed (>= 0)
+  unsigned int* err;            // error flags (bit 0: non-finite wave speed)
+  double* diag;                 // per-cell diagnostic partial sums [e][2]
+};
+
+// One RK stage update: Qnew = sum_j c[j]*src[j] + cQ*Q + cR*R (+ cR0*R0), with
+// optional copies of the old state, the new state and the residual.
+struct RKStage {
+  const double* src[3];
+  double c[3];
+  int nsrc;
+  int pad;
+  double cQ, cR, cR0;
+  const double* R0;
+  double* save_old;
+  double* save_new;
+  double* save_R;
+  int write_resid;  // also store the residual in SolveDev::resid
+  int diag;         // accumulate sum(resid^2) per cell into diag[e][0]
+};
+
+// launch helpers implemented in kernels_*.cu (one translation unit per N)
+struct Launch {
+  int epb;    // cells per CTA in element kernels
+  int threads;
+};
+
+template <int N> void launch_e1(const SolveDev& s, const Launch& L, cudaStream_t st);
+template <int N> void launch_f1(const SolveDev& s, cudaStream_t st);
+template <int N> void launch_e2(const SolveDev& s, const Launch& L, cudaStream_t st);
+template <int N> void launch_f2(const SolveDev& s, cudaStream_t st);
+template <int N> void launch_e3(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st);
+template <int N> void launch_ct(const SolveDev& s, const Launch& L, cudaStream_t st, int mode);
+template <int N> void launch_nqsp(const SolveDev& s, int v0, int v1, cudaStream_t st);
+template <int N> void launch_divb(const SolveDev& s, cudaStream_t st);
+
+void upload_operators(int N, const double* Lmat, const double* Mmat, const double* Xs, const double* Xf,
+                      const double* Aav);
+void launch_point_rusanov(int n, double gam, const double* Qfl, const double* Qfr, double* Fnl, double* Fnr,
+                          double* Az, const double* normf, const int* sl, const int* sr, double* ev,
+                          cudaStream_t st);
+void launch_point_iflux(int n, double gam, const double* Qi, double* Fi, double* Gi, cudaStream_t st);
+void launch_point_vflux(int n, double gam, double mu, double eta0, const double* Qv, const double* nQ, double* Fv,
+                        double* Gv, cudaStream_t st);
+void launch_reduce_diag(const double* diag, int NC, double* out2, cudaStream_t st);
+
+}  // namespace chorus

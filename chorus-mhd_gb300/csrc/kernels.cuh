@@ -1,0 +1,624 @@
+// kernels.cuh -- stage kernels of the residual-and-time-step path, templated on N.
+//
+// One RK stage (compresid.f90:1-67 + the stage update of iterations.f90:162-217) is
+// five launches, one per grid-wide dependency level of the reference's compflux:
+//   E1  cell pass  Q -> flux-point values (all 2N(N+1) points), interior inviscid
+//                  flux, interior A_z, AV sensor           inviscid_flux_interior,
+//                                                          comp_artificial_viscosity
+//   F1  face pass  Rusanov flux on every face point, upwinded A_z, face-averaged Q,
+//                  max wave speed                          interfaceflux, CYCLOCFLUX,
+//                                                          BCFLUX, getrusanovflux
+//   E2  cell pass  grad Q (vars 1-8) and grad A_z at the solution points, grad Q at
+//                  every flux point                        nablaAsp, nablaQsp,
+//                                                          nablaQ_interior_FP
+//   F2  face pass  face-averaged grad Q, face AV viscosity interfaceVISflux,
+//                                                          BCVISFLUX, CYCLOCVISFLUX,
+//                                                          compAVflux
+//   E3  cell pass  viscous + AV flux, divergence, A_z advection, RK update
+//                                                          comp_viscous_flux,
+//                                                          compresid, RK_S5P3
+// Cell passes stage a block of `epb` cells in shared memory; face passes run one
+// thread per face point.  All arithmetic is FP64.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "chorus_internal.h"
+#include "physics.cuh"
+
+namespace chorus {
+
+struct OpsN {
+  double L[(kMaxN + 1) * kMaxN];  // Lmat(N+1,N) column-major
+  double M[(kMaxN + 1) * kMaxN];  // Mmat(N+1,N)
+  double A[kMaxN * kMaxN];        // AV smoothing operator A[i*N+m] (projection to N-1 points and back)
+  double Xf[kMaxN + 1];
+  double Xs[kMaxN];
+};
+
+// one copy per translation unit; upload_ops_tu() fills it
+static __constant__ OpsN c_ops;
+
+template <int N>
+struct D {
+  static constexpr int NS = N * N;
+  static constexpr int NF1 = (N + 1) * N;
+  static constexpr int NFP = 2 * NF1;
+  static constexpr int NG = 4 * (N + 1);  // gradient weights per solution point
+};
+
+// element-local flux-point index of face point nfp (0-based) of local face lf (1..4),
+// from face2fpconnec (initsetup.f90:343-379)
+template <int N>
+__device__ __forceinline__ int face_fp(int lf, int nfp) {
+  constexpr int NF1 = D<N>::NF1;
+  switch (lf) {
+    case 1: return NF1 + nfp;                   // family 2, ifp = nfp,     jfp = 1
+    case 2: return nfp * (N + 1) + N;           // family 1, ifp = N+1,     jfp = nfp
+    case 3: return NF1 + N * N + (N - 1 - nfp); // family 2, ifp = N-nfp+1, jfp = N+1
+    default: return (N - 1 - nfp) * (N + 1);    // family 1, ifp = 1,       jfp = N-nfp+1
+  }
+}
+
+__device__ __forceinline__ unsigned long long ev_bits(double ev, unsigned int* err) {
+  if (!(ev >= 0.0) || ev > 1.0e300) {  // NaN or inf wave speed: non-physical state
+    atomicOr(err, 1u);
+    return 0ull;
+  }
+  return (unsigned long long)__double_as_longlong(ev);
+}
+
+__device__ __forceinline__ void block_max_ull(unsigned long long v, unsigned long long* out) {
+  __shared__ unsigned long long red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? red[lane] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = w > v ? w : v;
+    }
+    if (lane == 0 && v) atomicMax(out, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// E1: flux-point values, interior inviscid flux, AV sensor
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor) {
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  double* sQ = sm;                    // [epb][NS][9]
+  double* sT = sQ + epb * NS * 9;     // [epb][NS] sensor scratch
+  double* sU = sT + epb * NS;         // [epb][NS]
+  {
+    const double* g = s.Q + (size_t)e0 * NS * 9;
+    for (int i = threadIdx.x; i < cnt * NS * 9; i += blockDim.x) sQ[i] = g[i];
+  }
+  __syncthreads();
+  const double gm1 = s.gam - 1.0;
+  for (int t = threadIdx.x; t < cnt * NFP; t += blockDim.x) {
+    const int e = t / NFP, fp = t - e * NFP;
+    const double* q = sQ + e * NS * 9;
+    double qf[9];
+    int lidx;
+    if (fp < NF1) {
+      const int ifp = fp % (N + 1), jfp = fp / (N + 1);
+      lidx = ifp;
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        double a = 0.0;
+#pragma unroll
+        for (int sp = 0; sp < N; sp++) a += q[(jfp * N + sp) * 9 + k] * c_ops.L[ifp + (N + 1) * sp];
+        qf[k] = a;
+      }
+    } else {
+      const int r = fp - NF1, ifp = r % N, jfp = r / N;
+      lidx = jfp;
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        double a = 0.0;
+#pragma unroll
+        for (int sp = 0; sp < N; sp++) a += q[(sp * N + ifp) * 9 + k] * c_ops.L[jfp + (N + 1) * sp];
+        qf[k] = a;
+      }
+    }
+    const size_t g = (size_t)(e0 + e) * NFP + fp;
+    double* dst = s.Qvf + g * 9;
+#pragma unroll
+    for (int k = 0; k < 9; k++) dst[k] = qf[k];
+    if (lidx > 0 && lidx < N) {
+      s.Azf[g] = qf[8];
+      const double sx = s.met[2 * g], sy = s.met[2 * g + 1];
+      double F[8];
+      iflux_contra(qf, sx, sy, gm1, F);
+      double* fo = s.Fc + g * 8;
+#pragma unroll
+      for (int k = 0; k < 8; k++) fo[k] = F[k];
+    }
+  }
+  if (!sensor) return;
+  // AV sensor of variable 1 (AV.f90:15-82): Qsm = A rho A^T, Se = log10 sum((Qsm-rho)/rho)^2
+  for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
+    const int e = t / NS, p = t - e * NS, is = p % N, n = p / N;
+    const double* q = sQ + e * NS * 9;
+    double a = 0.0;
+#pragma unroll
+    for (int m = 0; m < N; m++) a += c_ops.A[is * N + m] * q[(n * N + m) * 9];
+    sT[e * NS + p] = a;  // T(is, n)
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
+    const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
+    double a = 0.0;
+#pragma unroll
+    for (int n = 0; n < N; n++) a += c_ops.A[js * N + n] * sT[e * NS + n * N + is];
+    const double rho = sQ[(e * NS + p) * 9];
+    const double d = a - rho;
+    sU[e * NS + p] = d * d / (rho * rho);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    double acc = 0.0;
+    for (int p = 0; p < NS; p++) acc += sU[e * NS + p];
+    s.Se[e0 + e] = log10(acc);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// F1: Rusanov flux on every face point (interfaceflux / CYCLOCFLUX / BCFLUX)
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(256) k_f1(SolveDev s) {
+  constexpr int NFP = D<N>::NFP;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n2 = s.nface2 * N, n1 = s.nface1 * N;
+  unsigned long long evb = 0ull;
+  if (t < n2 + n1) {
+    const bool two = t < n2;
+    const int tt = two ? t : t - n2;
+    const int f = tt / N, nfp = tt - f * N;
+    size_t gl, gr = 0;
+    FaceNorm fn;
+    if (two) {
+      const int4 fc = s.face2[f];
+      gl = (size_t)fc.x * NFP + face_fp<N>(fc.y, nfp);
+      gr = (size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp);
+      fn = s.fn2[tt];
+    } else {
+      const int2 fc = s.face1[f];
+      gl = (size_t)fc.x * NFP + face_fp<N>(fc.y, nfp);
+      fn = s.fn1[tt];
+    }
+    double ql[9], qr[9];
+    const double* pl = s.Qvf + gl * 9;
+#pragma unroll
+    for (int k = 0; k < 9; k++) ql[k] = pl[k];
+    if (two) {
+      const double* pr = s.Qvf + gr * 9;
+#pragma unroll
+      for (int k = 0; k < 9; k++) qr[k] = pr[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; k++) qr[k] = ql[k];
+    }
+    double Fh[8], vnl, ev;
+    rusanov_core(ql, qr, fn.ux, fn.uy, s.gam, Fh, vnl, ev);
+    evb = ev_bits(ev, s.err);
+    const double az = vnl > 0.0 ? ql[8] : qr[8];
+    double* fl = s.Fc + gl * 8;
+#pragma unroll
+    for (int k = 0; k < 8; k++) fl[k] = fn.msl * Fh[k];
+    s.Azf[gl] = az;
+    if (two) {
+      double* fr = s.Fc + gr * 8;
+#pragma unroll
+      for (int k = 0; k < 8; k++) fr[k] = fn.ss * (fn.msl * Fh[k]);
+      s.Azf[gr] = az;
+      double* al = s.Qvf + gl * 9;
+      double* ar = s.Qvf + gr * 9;
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        const double a = 0.5 * ql[k] + 0.5 * qr[k];
+        al[k] = a;
+        ar[k] = a;
+      }
+    }
+  }
+  block_max_ull(evb, s.eig);
+}
+
+// ---------------------------------------------------------------------------
+// E2: gradients at solution points and their values at every flux point
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb) {
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  double* sQ = sm;                  // [epb][NFP][9]
+  double* sA = sQ + epb * NFP * 9;  // [epb][NFP]
+  double* sG = sA + epb * NFP;      // [epb][NS][16]  (d*8 + k)
+  {
+    const double2* g = reinterpret_cast<const double2*>(s.Qvf + (size_t)e0 * NFP * 9);
+    double2* d = reinterpret_cast<double2*>(sQ);
+    const int n2 = cnt * NFP * 9 / 2;  // NFP even
+    for (int i = threadIdx.x; i < n2; i += blockDim.x) d[i] = g[i];
+    const double* ga = s.Azf + (size_t)e0 * NFP;
+    for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) sA[i] = ga[i];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
+    const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
+    const double* w = s.gco + ((size_t)(e0 + e) * NS + p) * NG;
+    double cx1[N + 1], cx2[N + 1], cy1[N + 1], cy2[N + 1];
+#pragma unroll
+    for (int r = 0; r <= N; r++) {
+      cx1[r] = w[r];
+      cx2[r] = w[(N + 1) + r];
+      cy1[r] = w[2 * (N + 1) + r];
+      cy2[r] = w[3 * (N + 1) + r];
+    }
+    const double* q = sQ + e * NFP * 9;
+    const size_t gs = (size_t)(e0 + e) * NS + p;
+    double* out = s.nQs + gs * 18;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      double gx = 0.0, gy = 0.0;
+#pragma unroll
+      for (int r = 0; r <= N; r++) {
+        const double a = q[(js * (N + 1) + r) * 9 + k];
+        const double b = q[(NF1 + r * N + is) * 9 + k];
+        gx += cx1[r] * a;
+        gx += cx2[r] * b;
+        gy += cy1[r] * a;
+        gy += cy2[r] * b;
+      }
+      out[k] = gx;
+      out[9 + k] = gy;
+      sG[(e * NS + p) * 16 + k] = gx;
+      sG[(e * NS + p) * 16 + 8 + k] = gy;
+    }
+    const double* az = sA + e * NFP;
+    double ax = 0.0, ay = 0.0;
+#pragma unroll
+    for (int r = 0; r <= N; r++) {
+      const double a = az[js * (N + 1) + r];
+      const double b = az[NF1 + r * N + is];
+      ax += cx1[r] * a;
+      ax += cx2[r] * b;
+      ay += cy1[r] * a;
+      ay += cy2[r] * b;
+    }
+    s.nAs[2 * gs] = ax;
+    s.nAs[2 * gs + 1] = ay;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < cnt * NFP; t += blockDim.x) {
+    const int e = t / NFP, fp = t - e * NFP;
+    const double* G = sG + e * NS * 16;
+    double acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) acc[c] = 0.0;
+    if (fp < NF1) {
+      const int ifp = fp % (N + 1), jfp = fp / (N + 1);
+#pragma unroll
+      for (int sp = 0; sp < N; sp++) {
+        const double l = c_ops.L[ifp + (N + 1) * sp];
+#pragma unroll
+        for (int c = 0; c < 16; c++) acc[c] += G[(jfp * N + sp) * 16 + c] * l;
+      }
+    } else {
+      const int r = fp - NF1, ifp = r % N, jfp = r / N;
+#pragma unroll
+      for (int sp = 0; sp < N; sp++) {
+        const double l = c_ops.L[jfp + (N + 1) * sp];
+#pragma unroll
+        for (int c = 0; c < 16; c++) acc[c] += G[(sp * N + ifp) * 16 + c] * l;
+      }
+    }
+    double* o = s.nQvf + ((size_t)(e0 + e) * NFP + fp) * 18;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      o[k] = acc[k];
+      o[9 + k] = acc[8 + k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// F2: face-averaged gradients and face AV viscosity
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(256) k_f2(SolveDev s, double eps_scale) {
+  constexpr int NFP = D<N>::NFP;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n2 = s.nface2 * N, n1 = s.nface1 * N;
+  const double eig = __longlong_as_double((long long)*s.eig);
+  const double eps0 = eig * s.hmsh / (double)(N - 1) * eps_scale;
+  if (t < n2) {
+    const int f = t / N, nfp = t - f * N;
+    const int4 fc = s.face2[f];
+    const size_t gl = (size_t)fc.x * NFP + face_fp<N>(fc.y, nfp);
+    const size_t gr = (size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp);
+    double* a = s.nQvf + gl * 18;
+    double* b = s.nQvf + gr * 18;
+#pragma unroll
+    for (int d = 0; d < 2; d++)
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const double v = 0.5 * a[9 * d + k] + 0.5 * b[9 * d + k];
+        a[9 * d + k] = v;
+        b[9 * d + k] = v;
+      }
+    if (nfp == 0) {
+      double m = 0.0;
+      if (s.artiv) m = 0.5 * (av_mu(s.Se[fc.x], eps0) + av_mu(s.Se[fc.z], eps0));
+      s.muf[4 * fc.x + fc.y - 1] = m;
+      s.muf[4 * fc.z + fc.w - 1] = m;
+    }
+  } else if (t < n2 + n1) {
+    const int tt = t - n2, f = tt / N, nfp = tt - f * N;
+    if (nfp == 0) {
+      const int2 fc = s.face1[f];
+      s.muf[4 * fc.x + fc.y - 1] = s.artiv ? av_mu(s.Se[fc.x], eps0) : 0.0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// E3: viscous + AV flux, divergence, A_z advection, RK update
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(256) k_e3(SolveDev s, RKStage rk, int epb, int update) {
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  double* sF = sm;                 // [epb][NFP][8] total flux Fv - F
+  double* sD = sF + epb * NFP * 8; // [epb][NS] diagnostic partial sums
+  const bool visc = true;
+  for (int t = threadIdx.x; t < cnt * NFP; t += blockDim.x) {
+    const int e = t / NFP, fp = t - e * NFP, c = e0 + e;
+    const size_t g = (size_t)c * NFP + fp;
+    double F[8];
+    const double* fi = s.Fc + g * 8;
+#pragma unroll
+    for (int k = 0; k < 8; k++) F[k] = -fi[k];
+    double mut = s.mu;
+    if (s.artiv) {
+      const double* mf = s.muf + 4 * c;
+      if (fp < NF1) {
+        const double x = c_ops.Xf[fp % (N + 1)];
+        mut += mf[3] * (1.0 - x) + mf[1] * x;
+      } else {
+        const double x = c_ops.Xf[(fp - NF1) / N];
+        mut += mf[0] * (1.0 - x) + mf[2] * x;
+      }
+    }
+    if (visc && (mut != 0.0 || s.eta0 != 0.0)) {
+      double q[9], gq[18], Fv[8];
+      const double* pq = s.Qvf + g * 9;
+      const double* pg = s.nQvf + g * 18;
+#pragma unroll
+      for (int k = 0; k < 8; k++) q[k] = pq[k];
+      q[8] = 0.0;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        gq[k] = pg[k];
+        gq[9 + k] = pg[9 + k];
+      }
+      gq[8] = 0.0;
+      gq[17] = 0.0;
+      vflux_contra(q, gq, mut, s.eta0, s.gam, s.met[2 * g], s.met[2 * g + 1], Fv);
+#pragma unroll
+      for (int k = 1; k < 8; k++) F[k] += Fv[k];
+    }
+    double* d = sF + (e * NFP + fp) * 8;
+#pragma unroll
+    for (int k = 0; k < 8; k++) d[k] = F[k];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
+    const int e = t / NS, p = t - e * NS, is = p % N, js = p / N, c = e0 + e;
+    const double* Fe = sF + e * NFP * 8;
+    double R[9];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      double a = 0.0;
+#pragma unroll
+      for (int r = 0; r <= N; r++) {
+        a += c_ops.M[r + (N + 1) * is] * Fe[(js * (N + 1) + r) * 8 + k];
+        a += c_ops.M[r + (N + 1) * js] * Fe[(NF1 + r * N + is) * 8 + k];
+      }
+      R[k] = a;
+    }
+    const size_t gs = (size_t)c * NS + p;
+    const double ij = s.invJ[gs];
+#pragma unroll
+    for (int k = 0; k < 8; k++) R[k] *= ij;
+    double* Qp = s.Q + gs * 9;
+    double q[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) q[k] = Qp[k];
+    const double ri = 1.0 / q[0];
+    const double ax = s.nAs[2 * gs] - s.B0y, ay = s.nAs[2 * gs + 1] + s.B0x;
+    R[8] = -(q[1] * ri * ax + q[2] * ri * ay);
+    if (rk.write_resid) {
+      double* ro = s.resid + gs * 9;
+#pragma unroll
+      for (int k = 0; k < 9; k++) ro[k] = R[k];
+    }
+    if (rk.diag) {
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < 9; k++) acc += R[k] * R[k];
+      sD[e * NS + p] = acc;
+    }
+    if (update) {
+      if (rk.save_old) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) rk.save_old[gs * 9 + k] = q[k];
+      }
+      if (rk.save_R) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) rk.save_R[gs * 9 + k] = R[k];
+      }
+      double qn[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) qn[k] = rk.cQ * q[k] + rk.cR * R[k];
+      for (int j = 0; j < rk.nsrc; j++) {
+        const double* sp = rk.src[j] + gs * 9;
+        const double cj = rk.c[j];
+#pragma unroll
+        for (int k = 0; k < 9; k++) qn[k] += cj * sp[k];
+      }
+      if (rk.R0) {
+        const double* r0 = rk.R0 + gs * 9;
+#pragma unroll
+        for (int k = 0; k < 9; k++) qn[k] += rk.cR0 * r0[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 9; k++) Qp[k] = qn[k];
+      if (rk.save_new) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) rk.save_new[gs * 9 + k] = qn[k];
+      }
+    }
+  }
+  if (rk.diag) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      double acc = 0.0;
+      for (int p = 0; p < NS; p++) acc += sD[e * NS + p];
+      s.diag[2 * (e0 + e)] = acc;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CT projection (correct_B_via_curl_Az, setinitialcond.f90:82-91)
+//   mode 0: A_z at every flux point (into Qvf variable 9)
+//   mode 2: grad A_z from the face-averaged values, B <- B0 + curl A_z
+// (mode 1, the face average, is k_ctface)
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(256) k_ct_elem(SolveDev s, int epb, int mode) {
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  double* sA = sm;  // mode 0: [epb][NS] A_z at solution points; mode 2: [epb][NFP]
+  if (mode == 0) {
+    for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sA[i] = s.Q[((size_t)e0 * NS + i) * 9 + 8];
+    __syncthreads();
+    for (int t = threadIdx.x; t < cnt * NFP; t += blockDim.x) {
+      const int e = t / NFP, fp = t - e * NFP;
+      const double* a = sA + e * NS;
+      double v = 0.0;
+      if (fp < NF1) {
+        const int ifp = fp % (N + 1), jfp = fp / (N + 1);
+#pragma unroll
+        for (int sp = 0; sp < N; sp++) v += a[jfp * N + sp] * c_ops.L[ifp + (N + 1) * sp];
+      } else {
+        const int r = fp - NF1, ifp = r % N, jfp = r / N;
+#pragma unroll
+        for (int sp = 0; sp < N; sp++) v += a[sp * N + ifp] * c_ops.L[jfp + (N + 1) * sp];
+      }
+      s.Qvf[((size_t)(e0 + e) * NFP + fp) * 9 + 8] = v;
+    }
+  } else {
+    for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) sA[i] = s.Qvf[((size_t)e0 * NFP + i) * 9 + 8];
+    __syncthreads();
+    for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
+      const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
+      const size_t gs = (size_t)(e0 + e) * NS + p;
+      const double* w = s.gco + gs * NG;
+      const double* a = sA + e * NFP;
+      double gx = 0.0, gy = 0.0;
+#pragma unroll
+      for (int r = 0; r <= N; r++) {
+        const double fa = a[js * (N + 1) + r], fb = a[NF1 + r * N + is];
+        gx += w[r] * fa;
+        gx += w[(N + 1) + r] * fb;
+        gy += w[2 * (N + 1) + r] * fa;
+        gy += w[3 * (N + 1) + r] * fb;
+      }
+      s.nQs[gs * 18 + 8] = gx;
+      s.nQs[gs * 18 + 9 + 8] = gy;
+      s.Q[gs * 9 + 5] = gy + s.B0x;
+      s.Q[gs * 9 + 6] = -gx + s.B0y;
+    }
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_ct_face(SolveDev s) {
+  constexpr int NFP = D<N>::NFP;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= s.nface2 * N) return;
+  const int f = t / N, nfp = t - f * N;
+  const int4 fc = s.face2[f];
+  const size_t gl = (size_t)fc.x * NFP + face_fp<N>(fc.y, nfp);
+  const size_t gr = (size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp);
+  const double v = 0.5 * s.Qvf[gl * 9 + 8] + 0.5 * s.Qvf[gr * 9 + 8];
+  s.Qvf[gl * 9 + 8] = v;
+  s.Qvf[gr * 9 + 8] = v;
+}
+
+// nablaQsp(v0..v1) (compflux.f90:107-157) from the current Qvf, 0-based variables
+template <int N>
+__global__ void __launch_bounds__(256) k_nqsp(SolveDev s, int v0, int v1) {
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= s.NC * NS) return;
+  const int c = t / NS, p = t - c * NS, is = p % N, js = p / N;
+  const double* w = s.gco + (size_t)t * NG;
+  const double* q = s.Qvf + (size_t)c * NFP * 9;
+  for (int k = v0; k <= v1; k++) {
+    double gx = 0.0, gy = 0.0;
+#pragma unroll
+    for (int r = 0; r <= N; r++) {
+      const double fa = q[(js * (N + 1) + r) * 9 + k], fb = q[(NF1 + r * N + is) * 9 + k];
+      gx += w[r] * fa;
+      gx += w[(N + 1) + r] * fb;
+      gy += w[2 * (N + 1) + r] * fa;
+      gy += w[3 * (N + 1) + r] * fb;
+    }
+    s.nQs[(size_t)t * 18 + k] = gx;
+    s.nQs[(size_t)t * 18 + 9 + k] = gy;
+  }
+}
+
+// per-cell sum of (dBx/dx + dBy/dy)^2 (iterations.f90:48) into diag[e][1]
+template <int N>
+__global__ void __launch_bounds__(256) k_divb(SolveDev s) {
+  constexpr int NS = D<N>::NS;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= s.NC) return;
+  double acc = 0.0;
+  for (int p = 0; p < NS; p++) {
+    const double* g = s.nQs + ((size_t)c * NS + p) * 18;
+    const double d = g[5] + g[9 + 6];
+    acc += d * d;
+  }
+  s.diag[2 * c + 1] = acc;
+}
+
+}  // namespace chorus

@@ -1,0 +1,85 @@
+// kernels_inst.cuh -- explicit instantiation of the stage kernels for N = CHORUS_N.
+// Each translation unit holds its own constant-memory copy of the N-point operators.
+#include "kernels.cuh"
+
+#ifndef CHORUS_N
+#error "define CHORUS_N before including kernels_inst.cuh"
+#endif
+#define CHORUS_CAT2(a, b) a##b
+#define CHORUS_CAT(a, b) CHORUS_CAT2(a, b)
+
+namespace chorus {
+
+namespace {
+constexpr int kN = CHORUS_N;
+inline size_t smem_e1(int epb) { return sizeof(double) * epb * (D<kN>::NS * 9 + 2 * D<kN>::NS); }
+inline size_t smem_e2(int epb) { return sizeof(double) * epb * (D<kN>::NFP * 9 + D<kN>::NFP + D<kN>::NS * 16); }
+inline size_t smem_e3(int epb) { return sizeof(double) * epb * (D<kN>::NFP * 8 + D<kN>::NS); }
+inline size_t smem_ct(int epb) { return sizeof(double) * epb * D<kN>::NFP; }
+inline int grid_cells(int nc, int epb) { return (nc + epb - 1) / epb; }
+
+void set_smem_limits() {
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && done[dev]) return;
+  const int lim = 200 * 1024;
+  cudaFuncSetAttribute(k_e1<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(k_e2<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(k_e3<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(k_ct_elem<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (dev < 64) done[dev] = true;
+}
+}  // namespace
+
+void CHORUS_CAT(upload_ops_n, CHORUS_N)(const OpsN& o) {
+  set_smem_limits();
+  cudaMemcpyToSymbol(c_ops, &o, sizeof(OpsN));
+}
+
+template <>
+void launch_e1<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
+  k_e1<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, s.artiv);
+}
+void CHORUS_CAT(launch_e1_nosensor_n, CHORUS_N)(const SolveDev& s, const Launch& L, cudaStream_t st) {
+  k_e1<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, 0);
+}
+template <>
+void launch_f1<kN>(const SolveDev& s, cudaStream_t st) {
+  const int n = (s.nface2 + s.nface1) * kN;
+  if (n > 0) k_f1<kN><<<(n + 255) / 256, 256, 0, st>>>(s);
+}
+template <>
+void launch_e2<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
+  k_e2<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e2(L.epb), st>>>(s, L.epb);
+}
+template <>
+void launch_f2<kN>(const SolveDev& s, cudaStream_t st) {
+  const int n = (s.nface2 + s.nface1) * kN;
+  if (n > 0) k_f2<kN><<<(n + 255) / 256, 256, 0, st>>>(s, 1.0);
+}
+template <>
+void launch_e3<kN>(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st) {
+  const int update = (rk.cQ != 0.0 || rk.cR != 0.0 || rk.nsrc > 0) ? 1 : 0;
+  k_e3<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e3(L.epb), st>>>(s, rk, L.epb, update);
+}
+template <>
+void launch_ct<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int mode) {
+  if (mode == 1) {
+    const int n = s.nface2 * kN;
+    if (n > 0) k_ct_face<kN><<<(n + 255) / 256, 256, 0, st>>>(s);
+  } else {
+    k_ct_elem<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_ct(L.epb), st>>>(s, L.epb, mode);
+  }
+}
+template <>
+void launch_nqsp<kN>(const SolveDev& s, int v0, int v1, cudaStream_t st) {
+  const int n = s.NC * D<kN>::NS;
+  k_nqsp<kN><<<(n + 255) / 256, 256, 0, st>>>(s, v0, v1);
+}
+template <>
+void launch_divb<kN>(const SolveDev& s, cudaStream_t st) {
+  k_divb<kN><<<(s.NC + 255) / 256, 256, 0, st>>>(s);
+}
+
+}  // namespace chorus

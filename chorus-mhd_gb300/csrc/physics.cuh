@@ -1,0 +1,146 @@
+// physics.cuh -- FP64 point physics shared by the stage kernels and the point
+// entry points.  Each function states the reference routine it computes; the algebra
+// is regrouped to spend fewer FP64 instructions (one reciprocal of rho per point,
+// contravariant fluxes formed directly, viscous and AV fluxes fused), so results
+// agree with the reference to rounding, not bit for bit.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace chorus {
+
+constexpr double kLambda = -2.0 / 3.0;  // setup2d.f90:70
+constexpr double kPrandt = 0.72;        // setup2d.f90:71
+
+// Contravariant ideal-MHD flux F*sx + G*sy of getIfluxvectors (getrusanov.f90:111-153)
+// as used by inviscid_flux_interior (compflux.f90:77-78, 96-97).
+__host__ __device__ __forceinline__ void iflux_contra(const double* q, double sx, double sy, double gm1,
+                                                      double* F) {
+  const double rho = q[0], ru = q[1], rv = q[2], rw = q[3], E = q[4], Bx = q[5], By = q[6], Bz = q[7];
+  const double ri = 1.0 / rho;
+  const double u = ru * ri, v = rv * ri, w = rw * ri;
+  const double B2 = Bx * Bx + By * By + Bz * Bz;
+  const double ke = ru * u + rv * v + rw * w;
+  const double pg = gm1 * (E - 0.5 * ke - 0.5 * B2);
+  const double pt = pg + 0.5 * B2;
+  const double Un = u * sx + v * sy;
+  const double Bn = Bx * sx + By * sy;
+  F[0] = ru * sx + rv * sy;
+  F[1] = ru * Un + pt * sx - Bx * Bn;
+  F[2] = rv * Un + pt * sy - By * Bn;
+  F[3] = rw * Un - Bz * Bn;
+  F[4] = (E + pt) * Un - (u * Bx + v * By + w * Bz) * Bn;
+  F[5] = Bx * Un - u * Bn;
+  F[6] = By * Un - v * Bn;
+  F[7] = Bz * Un - w * Bn;
+}
+
+// Rusanov flux of getrusanovflux (getrusanov.f90:1-109) before the transform to the
+// computational frame: Fh = 0.5*(Fl + Fr - eigv*(qr - ql)) along the unit normal
+// (ux,uy); returns the left normal velocity (for the A_z upwinding, :99-103) and the
+// wave-speed bound eigv (:87).
+__host__ __device__ __forceinline__ void rusanov_core(const double* ql, const double* qr, double ux, double uy,
+                                                      double gam, double* Fh, double& vnl, double& eigv) {
+  const double gm1 = gam - 1.0;
+  double Fl[8], Fr[8], pgl, pgr, vn[2];
+  const double* qs[2] = {ql, qr};
+  double* Fs[2] = {Fl, Fr};
+  double* pg[2] = {&pgl, &pgr};
+#pragma unroll
+  for (int side = 0; side < 2; side++) {
+    const double* q = qs[side];
+    double* F = Fs[side];
+    const double ri = 1.0 / q[0];
+    const double u = ri * q[1], v = ri * q[2], w = ri * q[3];
+    const double Bx = q[5], By = q[6], Bz = q[7];
+    const double B2 = Bx * Bx + By * By + Bz * Bz;
+    const double p = gm1 * (q[4] - 0.5 * q[0] * (u * u + v * v + w * w) - B2 * 0.5);
+    const double pt = p + 0.5 * B2;
+    const double Vn = u * ux + v * uy;
+    const double Bn = Bx * ux + By * uy;
+    F[0] = q[0] * Vn;
+    F[1] = q[1] * Vn + pt * ux - Bx * Bn;
+    F[2] = q[2] * Vn + pt * uy - By * Bn;
+    F[3] = q[3] * Vn - Bz * Bn;
+    F[4] = (q[4] + pt) * Vn - Bn * (u * Bx + v * By + w * Bz);
+    F[5] = (v * Bx - u * By) * uy;
+    F[6] = (u * By - v * Bx) * ux;
+    F[7] = Bz * Vn - w * Bn;
+    *pg[side] = p;
+    vn[side] = Vn;
+  }
+  const double Bx = 0.5 * (ql[5] + qr[5]), By = 0.5 * (ql[6] + qr[6]), Bz = 0.5 * (ql[7] + qr[7]);
+  const double irs = 1.0 / (ql[0] + qr[0]);
+  const double ca = gam * (pgl + pgr) * irs;
+  const double cd = (Bx * Bx + By * By + Bz * Bz) * (2.0 * irs);
+  const double bn = Bx * ux + By * uy;
+  const double cn = bn * bn * (2.0 * irs);
+  const double cad = ca + cd;
+  const double ctmp = sqrt(cad * cad - 4.0 * ca * cn);
+  const double cf = sqrt(0.5 * (cad + ctmp));
+  eigv = 0.5 * fabs(vn[0] + vn[1]) + cf;
+#pragma unroll
+  for (int k = 0; k < 8; k++) Fh[k] = 0.5 * (Fl[k] + Fr[k] - eigv * (qr[k] - ql[k]));
+  vnl = vn[0];
+}
+
+// Contravariant viscous + resistive + artificial-viscosity flux at one flux point:
+// getVfluxvectors (getrusanov.f90:157-249) with (mu, eta0) plus getVfluxvectors_AV
+// (:251-360) with (mu_art, 0), summed (the hydrodynamic terms are linear in the
+// viscosity) and contracted with the metric row (sx, sy) as in comp_viscous_flux
+// (compflux.f90:216-225, 241-250).  g is nablaQ(9,2) in Fortran order; only
+// components 1..7 of the result are nonzero (Fv(1) = Fv(9) = 0).
+__host__ __device__ __forceinline__ void vflux_contra(const double* q, const double* g, double mut, double eta0,
+                                                      double gam, double sx, double sy, double* Fc) {
+  const double rho = q[0], Bx = q[5], By = q[6], Bz = q[7];
+  const double ri = 1.0 / rho;
+  const double u = q[1] * ri, v = q[2] * ri, w = q[3] * ri;
+  const double NU = u * u + v * v + w * w;
+  const double B2 = Bx * Bx + By * By + Bz * Bz;
+  const double inte = (q[4] - 0.5 * NU * rho - 0.5 * B2) * ri;
+  double du[2], dv[2], dw[2], de[2];
+#pragma unroll
+  for (int d = 0; d < 2; d++) {
+    const double* gd = g + 9 * d;
+    const double dr = gd[0];
+    du[d] = (gd[1] - dr * u) * ri;
+    dv[d] = (gd[2] - dr * v) * ri;
+    dw[d] = (gd[3] - dr * w) * ri;
+    const double dke = 0.5 * NU * dr + rho * (u * du[d] + v * dv[d] + w * dw[d]);
+    const double dpb = Bx * gd[5] + By * gd[6] + Bz * gd[7];
+    de[d] = (gd[4] - dke - dpb - dr * inte) * ri;
+  }
+  const double ux = du[0], uy = du[1], vx = dv[0], vy = dv[1];
+  const double div = ux + vy;
+  const double kq = mut * gam / kPrandt;
+  const double f1 = mut * (2.0 * ux + kLambda * div);
+  const double f2 = mut * (vx + uy);
+  const double f3 = mut * dw[0];
+  const double g2 = mut * (2.0 * vy + kLambda * div);
+  const double g3 = mut * dw[1];
+  double f4 = u * f1 + v * f2 + w * f3 + kq * de[0];
+  double g4 = f2 * u + g2 * v + g3 * w + kq * de[1];
+  // resistive terms (eta0 only; the AV form has eta_art = 0)
+  const double Jx = g[9 + 7], Jy = -g[7], Jz = g[6] - g[9 + 5];
+  const double f6 = eta0 * Jz, f7 = -eta0 * Jy;
+  const double g5 = -eta0 * Jz, g7 = eta0 * Jx;
+  f4 = f4 + f6 * By + f7 * Bz;
+  g4 = g4 + g5 * Bx + g7 * Bz;
+  Fc[0] = 0.0;
+  Fc[1] = f1 * sx + f2 * sy;
+  Fc[2] = f2 * sx + g2 * sy;
+  Fc[3] = f3 * sx + g3 * sy;
+  Fc[4] = f4 * sx + g4 * sy;
+  Fc[5] = g5 * sy;
+  Fc[6] = f6 * sx;
+  Fc[7] = f7 * sx + g7 * sy;
+}
+
+// muAV of variable 1 from the sensor (AV.f90:157-172 with se_low=-6, se_high=-1).
+__host__ __device__ __forceinline__ double av_mu(double se, double eps0) {
+  if (se < -6.0) return 0.0;
+  if (se > -1.0) return eps0;
+  const double s0 = -3.5, kr = 2.5, pi = 3.14159265358979323846;
+  return eps0 / 2.0 * (1.0 + sin(pi * (se - s0) / 2.0 / kr));
+}
+
+}  // namespace chorus

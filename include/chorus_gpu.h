@@ -1,0 +1,179 @@
+/*
+ * chorus_gpu.h -- C-ABI of libchorus_gpu.so, the GB300 (sm_103a) implementation of
+ * CHORUS-MHD's residual-and-time-step hot path.
+ *
+ * The reference's hot-path routines are external Fortran subroutines that talk
+ * through module `setup2d` globals.  A Fortran host binds its setup2d arrays once
+ * (chorus_gpu_bind), then calls the `_gpu` drop-ins where it used to CALL the CPU
+ * routines; each drop-in keeps the routine's name and argument meaning, with the
+ * module state replaced by an explicit context.  Every function returns 0 on success
+ * and a nonzero CHORUS_E* code on failure; chorus_gpu_last_error() gives the message
+ * (the reference prints and STOPs instead).
+ *
+ * Layout contract: every array is passed exactly as the Fortran host holds it --
+ * column-major, first index fastest, integer maps with 1-based values, INTEGER =
+ * int32, DOUBLE PRECISION = double.  The caller keeps ownership of its arrays.
+ */
+#ifndef CHORUS_GPU_H
+#define CHORUS_GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  CHORUS_OK = 0,
+  CHORUS_EINVAL = 1,   /* bad argument / size out of range */
+  CHORUS_ECUDA = 2,    /* CUDA runtime error */
+  CHORUS_EMESH = 3,    /* mesh/connectivity inconsistency (connectivity.f90 STOP paths) */
+  CHORUS_EIO = 4,      /* file I/O */
+  CHORUS_ESTATE = 5,   /* non-finite or non-physical state flagged by a kernel */
+  CHORUS_ENOMEM = 6,   /* device memory budget exceeded */
+};
+
+/* Sizes of one single-partition solve (setup2d.f90:19-21). */
+typedef struct ChorusDims {
+  int32_t N;      /* solution points per direction, 2..8 (setup2d.f90:47) */
+  int32_t NCELL;  /* cells */
+  int32_t NFACE;  /* faces (rows of IF2C) */
+  int32_t NINTER; /* interior faces (IBFINTER) */
+  int32_t NFREE;  /* FREE boundary faces (IBFREE) */
+  int32_t NPAIR;  /* local periodic face pairs (CYC2FPAIR) */
+} ChorusDims;
+
+/* Physical and run parameters (setup2d.f90:63-81, readinput.f90:17-30).  gam is a
+ * compile-time parameter in the reference (5/3, setup2d.f90:68); here it is runtime.
+ * B0x/B0y: uniform background field with A_z = A_bg + dA_z, B = B0 + curl(dA_z);
+ * zero reproduces the reference exactly. */
+typedef struct ChorusParams {
+  double gam, mu, eta0;
+  double DXCYCL, DYCYCL;  /* used only for the AV length scale (AV.f90:147) */
+  double dt;
+  double B0x, B0y;
+  int32_t NCELLGLOB;
+  int32_t vismode;  /* must be 1 (the reference reads Qvfi/Azfi only when vismode==1) */
+  int32_t ARTIV;    /* 1: artificial viscosity on */
+  int32_t k_stage;  /* 3: RK_S5P3, 5: FiveStageRk */
+} ChorusParams;
+
+/* Diagnostics of iterations.f90:39-76, produced when mod(iter,10)==1. */
+typedef struct ChorusDiag {
+  int32_t iter;
+  int32_t pad;
+  double ctime;
+  double residglob; /* sqrt(sum resid^2 / (NCELLGLOB*N*N*5)) */
+  double divBglob;  /* sqrt(sum (dBx/dx+dBy/dy)^2 / (NCELLGLOB*N*N)) */
+  double eigvmax_g; /* global max Rusanov wave speed of the last stage (AV.f90:145) */
+  double epsilon0;  /* AV amplitude of the last stage (AV.f90:148) */
+} ChorusDiag;
+
+typedef struct ChorusCtx ChorusCtx;
+typedef struct ChorusMesh ChorusMesh;
+typedef struct ChorusBatch ChorusBatch;
+
+/* Thread-local message of the last failing call. */
+const char* chorus_gpu_last_error(void);
+/* Library version string. */
+const char* chorus_gpu_version(void);
+
+/* ------------------------------------------------------------------------------
+ * Binding (replaces the module state set up by INIT_SETUP, initsetup.f90:1-165)
+ * --------------------------------------------------------------------------- */
+/* Copy maps, operators and metrics to `device` and allocate the resident state and
+ * work arrays.  Arrays (Fortran layout):
+ *   IF2C(NFACE,4), IBFINTER(NINTER), IBFREE(NFREE), CYC2FPAIR(NPAIR,2),
+ *   iface2fp(N,4), jface2fp(N,4)               -- connectivity.f90, connect_bdry.f90,
+ *                                                 map_cyc_loc.f90, initsetup.f90:343
+ *   Xs(N), Xf(N+1), Lmat(N+1,N), Mmat(N+1,N)   -- initsetup.f90:167-315
+ *   S1(2,2,N+1,N,NCELL), S2(2,2,N,N+1,NCELL), Jac(N,N,NCELL) -- calcjacob.f90:1-86 */
+int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* IBFINTER,
+                    const int32_t* IBFREE, const int32_t* CYC2FPAIR, const int32_t* iface2fp,
+                    const int32_t* jface2fp, const double* Xs, const double* Xf, const double* Lmat,
+                    const double* Mmat, const double* S1, const double* S2, const double* Jac,
+                    const ChorusParams* params, int32_t device, ChorusCtx** ctx);
+int chorus_gpu_free(ChorusCtx* ctx);
+/* Change dt / mu / eta0 / ARTIV of a bound context (setup2d.f90:72,77,81). */
+int chorus_gpu_set_params(ChorusCtx* ctx, const ChorusParams* params);
+
+/* Resident state Q(9,N,N,NCELL) (setup2d.f90:54). */
+int chorus_gpu_upload_state(ChorusCtx* ctx, const double* Q);
+int chorus_gpu_download_state(ChorusCtx* ctx, double* Q);
+/* Copy a named work array back in the reference layout, for parity checks:
+ * "resid" (9,N,N,NC), "F1" (8,N+1,N,NC), "G2" (8,N,N+1,NC), "Qvfi"/"Qvfj" (9,..),
+ * "Azfi"/"Azfj", "nablaQs" (9,2,N,N,NC), "nablaQvfi"/"nablaQvfj" (9,2,..),
+ * "nablaAs" (2,N,N,NC), "muAVfi"/"muAVfj" (9,2,NC; only variable 1 is carried),
+ * "SM_IND1" (NC; sensor of variable 1).  `count` must equal the array size. */
+int chorus_gpu_download_array(ChorusCtx* ctx, const char* name, double* out, int64_t count);
+/* eigvmax of the last stage (AV.f90:145) and epsilon0 (AV.f90:148). */
+int chorus_gpu_get_eigvmax(ChorusCtx* ctx, double* eigvmax_g, double* epsilon0);
+
+/* ------------------------------------------------------------------------------
+ * Drop-ins (reference routine -> GPU entry point)
+ * --------------------------------------------------------------------------- */
+/* compresid.f90:1-67 (calls compflux.f90:1-31 and everything below it); the result
+ * stays on the device in "resid". */
+int compresid_gpu(ChorusCtx* ctx);
+/* compflux.f90:33-49 comp_inviscid_flux (F1/G2, Qvfi/Qvfj, Azfi/Azfj, eigvmax). */
+int comp_inviscid_flux_gpu(ChorusCtx* ctx);
+/* compflux.f90:107-157 nablaQsp(v_sta,v_end) on the current Qvfi/Qvfj (1-based
+ * variable range, by reference like the Fortran call). */
+int nablaqsp_gpu(ChorusCtx* ctx, const int32_t* v_sta, const int32_t* v_end);
+/* setinitialcond.f90:82-91 correct_B_via_curl_Az (CT projection B <- curl A_z). */
+int correct_b_via_curl_az_gpu(ChorusCtx* ctx);
+/* iterations.f90:162-217 RK_S5P3 and :92-160 FiveStageRk: one 5-stage step with the
+ * bound dt; *ctime is advanced exactly as the reference does. */
+int rk_s5p3_gpu(ChorusCtx* ctx, double* ctime);
+int fivestagerk_gpu(ChorusCtx* ctx, double* ctime);
+/* iterations.f90:19-87 without output: nsteps x (RK step by k_stage, CT projection,
+ * norms when mod(iter,10)==1).  *iter and *ctime are advanced; up to max_diag
+ * diagnostic records are written to diag (may be NULL) and their number to *n_diag.
+ * The whole step is replayed from a CUDA graph. */
+int iterations_gpu(ChorusCtx* ctx, int32_t nsteps, int32_t* iter, double* ctime, ChorusDiag* diag,
+                   int32_t max_diag, int32_t* n_diag);
+
+/* Point functions with the reference argument lists, evaluated on the device over n
+ * points (host arrays, row i at offset i*stride): getrusanov.f90:1-109, :111-153,
+ * :157-249 and :251-360 (the AV form is getvfluxvectors with mu=mu_art, eta0=0). */
+int getrusanovflux_gpu(int32_t n, double gam, const double* Qfl /*n x 9*/, const double* Qfr /*n x 9*/,
+                       double* Fnl /*n x 8*/, double* Fnr /*n x 8*/, double* Az /*n*/,
+                       const double* normf /*n x 2*/, const int32_t* sign_l, const int32_t* sign_r,
+                       double* eigv /*n*/);
+int getifluxvectors_gpu(int32_t n, double gam, const double* Qi /*n x 8*/, double* Fi /*n x 8*/,
+                        double* Gi /*n x 8*/);
+int getvfluxvectors_gpu(int32_t n, double gam, double mu, double eta0, const double* Qv /*n x 9*/,
+                        const double* nablaQ /*n x 18, (9,2) per point*/, double* Fv /*n x 9*/,
+                        double* Gv /*n x 9*/);
+
+/* ------------------------------------------------------------------------------
+ * Host-side setup for callers without the Fortran setup chain: reads QUAD.INP and
+ * the .CEL/.VRT/.BND files and rebuilds the reference's maps (readinput.f90,
+ * readGRIDinfo.f90, CHECK_MESH/CONNECTIVITY connectivity.f90, CONNECT_BDRY
+ * connect_bdry.f90, MAPCYCLOC map_cyc_loc.f90) and geometry (initsetup.f90,
+ * mapder.f90, calcjacob.f90).  The integer maps are bit-identical to the
+ * reference's; the geometry follows its evaluation order.
+ * --------------------------------------------------------------------------- */
+int chorus_mesh_load(const char* case_dir, ChorusMesh** mesh);
+int chorus_mesh_free(ChorusMesh* mesh);
+/* dims/params as read; *maxiter = MAXITER, *problem = 0 OT, 1 rotor, 2 Alfven. */
+int chorus_mesh_info(const ChorusMesh* mesh, ChorusDims* dims, ChorusParams* params, int32_t* maxiter,
+                     int32_t* problem);
+/* Named arrays: int -- IF2C IC2F IF2V IVCELL IBFINTER IBFREE IBFCYC IBFCYCLOC CYC2FPAIR
+ * iface2fp jface2fp; double -- XV YV Xs Xf Lmat Mmat S1 S2 Jac XXsolu. */
+const int32_t* chorus_mesh_iarray(const ChorusMesh* mesh, const char* name, int64_t* count);
+const double* chorus_mesh_darray(const ChorusMesh* mesh, const char* name, int64_t* count);
+/* Bind a loaded mesh (chorus_gpu_bind with the mesh's arrays). */
+int chorus_gpu_bind_mesh(const ChorusMesh* mesh, int32_t device, ChorusCtx** ctx);
+/* SETINITIALCOND (setinitialcond.f90:1-80): analytic data at the solution points,
+ * CT projection on the device, energy rebuilt from the projected B; the state is
+ * left resident in ctx and also returned in Q (may be NULL). */
+int chorus_initial_state(const ChorusMesh* mesh, ChorusCtx* ctx, double* Q);
+
+/* Restart stream of write_data.f90:5-83 / read_data_restart.f90:35-67: int32 iter,
+ * float64 ctime, then per cell int32 global id + Q(9,N,N). */
+int chorus_write_restart(ChorusCtx* ctx, const char* path, int32_t iter, double ctime);
+int chorus_read_restart(ChorusCtx* ctx, const char* path, int32_t* iter, double* ctime);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

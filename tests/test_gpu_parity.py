@@ -1,0 +1,125 @@
+"""CUDA path vs the oracle on the same inputs (through the C-ABI).
+
+Tolerances: FP64 throughout; the kernels regroup the reference's algebra (fused
+multiply-adds, one reciprocal per point, precomputed metric weights), so single-stage
+arrays agree to ~1e-13 relative and whole runs to the stated 1e-10 relative L2.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from chorus_mhd import Mesh, Solver, reference_layout_sizes
+from helpers import assert_close, make_case, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+STAGE_TOL = 1e-12   # one compresid, normwise relative
+RUN_TOL = 1e-10     # whole run, relative L2 of Q (the stated bar)
+
+CASES = [
+    dict(problem="orszag_tang", nx=6, ny=6, N=4, jitter=0.0),
+    dict(problem="orszag_tang", nx=5, ny=7, N=3, jitter=0.15, seed=2),
+    dict(problem="orszag_tang", nx=4, ny=4, N=5, jitter=0.15, seed=3),
+    dict(problem="orszag_tang", nx=4, ny=3, N=6, jitter=0.1, seed=4),
+    dict(problem="orszag_tang", nx=3, ny=3, N=2, jitter=0.0),
+    dict(problem="orszag_tang", nx=3, ny=4, N=7, jitter=0.1, seed=5),
+    dict(problem="orszag_tang", nx=3, ny=3, N=8, jitter=0.0),
+    dict(problem="rotor", nx=64, ny=64, N=3, jitter=0.1, seed=6),
+    dict(problem="alfven", nx=6, ny=5, N=4, jitter=0.0),
+    dict(problem="orszag_tang", nx=6, ny=6, N=4, jitter=0.1, mu=0.01, eta0=0.02, seed=7),
+    dict(problem="orszag_tang", nx=5, ny=5, N=4, jitter=0.0, artiv=0),
+]
+
+
+def ids(c):
+    return "%s-%dx%d-N%d-j%s%s" % (c["problem"], c["nx"], c["ny"], c["N"], c.get("jitter", 0),
+                                 "-visc" if c.get("mu") else "" + ("-noav" if c.get("artiv") == 0 else ""))
+
+
+@pytest.mark.parametrize("case", CASES, ids=ids)
+def test_initial_state_matches_oracle(case_root, case):
+    d = make_case(case_root, **case)
+    o = oracle.Oracle(d)
+    s = Solver(Mesh(d))
+    assert_close(s.state(), o.array("Q"), 1e-13, "initial Q")
+
+
+@pytest.mark.parametrize("case", CASES, ids=ids)
+def test_one_stage_arrays_match_oracle(case_root, case):
+    """compresid on identical input: every intermediate array of compflux."""
+    d = make_case(case_root, **case)
+    o = oracle.Oracle(d)
+    o.run(2)  # move away from the symmetric initial data
+    Q = o.array("Q").copy()
+    s = Solver(Mesh(d), initial_state=False)
+    s.upload(Q)
+    o.compresid()
+    s.compresid()
+    sz = reference_layout_sizes(s.N, s.ncell)
+    for name in ["F1", "G2", "Qvfi", "Qvfj", "Azfi", "Azfj", "nablaAs", "resid"]:
+        assert_close(s.array(name, sz[name]), o.array(name), STAGE_TOL, name)
+    for name in ["nablaQs", "nablaQvfi", "nablaQvfj"]:
+        a = s.array(name, sz[name]).reshape(-1, 9)[:, :8]
+        b = o.array(name).reshape(-1, 9)[:, :8]
+        assert_close(a, b, STAGE_TOL, name)
+    if case.get("artiv", 1):
+        for name in ["muAVfi", "muAVfj"]:
+            a = s.array(name, sz[name]).reshape(-1, 9)[:, 0]
+            b = o.array(name).reshape(-1, 9)[:, 0]
+            assert np.allclose(a, b, rtol=1e-11, atol=1e-14 * max(1.0, np.abs(b).max())), name
+        # the sensor only matters through muAV: below -6 the viscosity is zero, so a
+        # smoothing that reproduces a constant density exactly (-inf) and one that
+        # leaves 1e-30 of round-off (-30) are the same answer
+        se = s.array("SM_IND1", s.ncell)
+        so = o.array("SM_IND").reshape(-1, 9)[:, 0]
+        assert np.array_equal(se >= -6.0, so >= -6.0)
+        live = so >= -12.0
+        assert np.allclose(se[live], so[live], rtol=0, atol=1e-8)
+    ev, eps = s.eigvmax()
+    assert abs(ev - o.getd("eigvmax")) <= 1e-13 * o.getd("eigvmax")
+
+
+@pytest.mark.parametrize("case", CASES, ids=ids)
+def test_run_matches_oracle(case_root, case):
+    """iterations: RK steps + CT projection + diagnostics vs the oracle."""
+    d = make_case(case_root, **case)
+    nsteps = 12
+    o = oracle.Oracle(d)
+    s = Solver(Mesh(d))
+    diag_o = []
+    for _ in range(nsteps):
+        r = o.step()
+        if r is not None:
+            diag_o.append(r)
+    diag_s = s.iterations(nsteps)
+    assert_close(s.state(), o.array("Q"), RUN_TOL, "Q after %d steps" % nsteps)
+    assert s.iter == o.geti("iter")
+    assert abs(s.ctime - o.getd("ctime")) <= 1e-15 * max(1.0, o.getd("ctime"))
+    assert len(diag_s) == len(diag_o) == 2
+    for a, (rg, db) in zip(diag_s, diag_o):
+        assert abs(a["residglob"] - rg) <= 1e-9 * rg
+        assert abs(a["divBglob"] - db) <= 1e-9 * db + 1e-13
+
+
+def test_fivestage_rk_matches_oracle(case_root):
+    d = make_case(case_root, problem="orszag_tang", nx=5, ny=5, N=4, jitter=0.1, k_stage=5, seed=9)
+    o = oracle.Oracle(d)
+    s = Solver(Mesh(d))
+    for _ in range(6):
+        o.step()
+    s.iterations(6)
+    assert_close(s.state(), o.array("Q"), RUN_TOL, "FiveStageRk")
+
+
+def test_drop_in_sequence_matches_oracle(case_root):
+    """RK_S5P3 + correct_B_via_curl_Az called one by one, like iterations.f90:22-33."""
+    d = make_case(case_root, problem="orszag_tang", nx=6, ny=5, N=4, jitter=0.1, seed=11)
+    o = oracle.Oracle(d)
+    s = Solver(Mesh(d))
+    for _ in range(3):
+        o.rk_s5p3()
+        o.correct_B_via_curl_Az()
+        s.RK_S5P3()
+        s.correct_B_via_curl_Az()
+    assert_close(s.state(), o.array("Q"), RUN_TOL, "drop-in sequence")
+    assert s.ctime == pytest.approx(o.getd("ctime"), rel=1e-15)

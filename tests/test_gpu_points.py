@@ -1,0 +1,86 @@
+"""Device point functions (getrusanovflux / getIfluxvectors / getVfluxvectors) vs
+the oracle's restatement, on random physical states."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from chorus_mhd import _lib
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def random_states(rng, n):
+    rho = rng.uniform(0.5, 3.0, n)
+    u = rng.uniform(-1, 1, (n, 3))
+    B = rng.uniform(-1, 1, (n, 3))
+    p = rng.uniform(0.2, 2.0, n)
+    gam = 5.0 / 3
+    Q = np.zeros((n, 9))
+    Q[:, 0] = rho
+    Q[:, 1:4] = rho[:, None] * u
+    Q[:, 4] = p / (gam - 1) + 0.5 * rho * (u ** 2).sum(1) + 0.5 * (B ** 2).sum(1)
+    Q[:, 5:8] = B
+    Q[:, 8] = rng.uniform(-1, 1, n)
+    return Q
+
+
+def test_rusanov_points():
+    rng = np.random.default_rng(0)
+    n = 500
+    gam = 5.0 / 3
+    Ql, Qr = random_states(rng, n), random_states(rng, n)
+    nf = rng.uniform(-2, 2, (n, 2))
+    sl = rng.choice([-1, 1], n).astype(np.int32)
+    sr = rng.choice([-1, 1], n).astype(np.int32)
+    Fl, Fr, Az, ev = np.zeros((n, 8)), np.zeros((n, 8)), np.zeros(n), np.zeros(n)
+    L = _lib.load()
+    _lib.check(L.getrusanovflux_gpu(n, gam, _dp(Ql), _dp(Qr), _dp(Fl), _dp(Fr), _dp(Az), _dp(nf), _ip(sl), _ip(sr),
+                                    _dp(ev)))
+    for i in range(n):
+        a, b, z, e = oracle.getrusanovflux(gam, Ql[i], Qr[i], nf[i], sl[i], sr[i])
+        sc = np.abs(a).max() + 1.0
+        assert np.abs(Fl[i] - a).max() <= TOL * sc
+        assert np.abs(Fr[i] - b).max() <= TOL * sc
+        assert Az[i] == z
+        assert abs(ev[i] - e) <= TOL * e
+
+
+def test_iflux_points():
+    rng = np.random.default_rng(1)
+    n = 300
+    gam = 1.4
+    Q = random_states(rng, n)[:, :8].copy()
+    F, G = np.zeros((n, 8)), np.zeros((n, 8))
+    L = _lib.load()
+    _lib.check(L.getifluxvectors_gpu(n, gam, _dp(Q), _dp(F), _dp(G)))
+    for i in range(n):
+        a, b = oracle.getifluxvectors(gam, Q[i])
+        assert np.abs(F[i] - a).max() <= TOL * (np.abs(a).max() + 1)
+        assert np.abs(G[i] - b).max() <= TOL * (np.abs(b).max() + 1)
+
+
+@pytest.mark.parametrize("mu,eta0", [(0.01, 0.0), (0.0, 0.03), (0.02, 0.05)])
+def test_vflux_points(mu, eta0):
+    rng = np.random.default_rng(2)
+    n = 300
+    gam = 5.0 / 3
+    Q = random_states(rng, n)
+    G = rng.uniform(-1, 1, (n, 18))
+    Fv, Gv = np.zeros((n, 9)), np.zeros((n, 9))
+    L = _lib.load()
+    _lib.check(L.getvfluxvectors_gpu(n, gam, mu, eta0, _dp(Q), _dp(G), _dp(Fv), _dp(Gv)))
+    for i in range(n):
+        a, b = oracle.getvfluxvectors(gam, mu, eta0, Q[i], G[i])
+        assert np.abs(Fv[i] - a).max() <= TOL * (np.abs(a).max() + 1e-300) + 1e-300
+        assert np.abs(Gv[i] - b).max() <= TOL * (np.abs(b).max() + 1e-300) + 1e-300

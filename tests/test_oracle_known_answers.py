@@ -1,0 +1,126 @@
+"""Pins of the oracle against analytic known answers.
+
+The reference ships no tests, fixtures or golden vectors and cannot be compiled on
+these machines, so the oracle (a loop-for-loop restatement) is pinned by facts that
+follow from the reference's own definitions:
+  * setsandpoints (initsetup.f90:174-253): Chebyshev-Gauss solution points and
+    Legendre-Gauss flux points plus end points;
+  * computeLandM (initsetup.f90:258-315): Lmat interpolates, Mmat differentiates
+    polynomials of degree <= N exactly;
+  * free-stream preservation of compresid on curved (jittered) cells;
+  * the unstaggered CT projection keeps the diagnostic div B at round-off on affine
+    meshes (iterations.f90:48,67);
+  * Orszag-Tang initial data of setinitialcond.f90:16-35;
+  * map invariants of CONNECTIVITY / CONNECT_BDRY / MAPCYCLOC.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import make_case
+
+
+@pytest.mark.parametrize("N", [2, 3, 4, 5, 6, 7, 8, 9, 10])
+def test_solution_and_flux_points(case_root, N):
+    d = make_case(case_root, problem="orszag_tang", nx=2, ny=2, N=N, steps=1) if N <= 8 else None
+    if d is None:
+        pytest.skip("the CUDA path stops at N=8; the oracle formulas are covered to N=8 here")
+    o = oracle.Oracle(d)
+    xs, xf = o.array("Xs"), o.array("Xf")
+    i = np.arange(1, N + 1)
+    assert np.allclose(xs, 0.5 * (1 - np.cos((2 * i - 1) * math.pi / (2 * N))), rtol=0, atol=2e-16)
+    g, _ = np.polynomial.legendre.leggauss(N - 1)
+    tol = 1e-15 if N <= 6 else 1e-12  # N>=7 nodes are 12-digit literals in the reference
+    assert xf[0] == 0.0 and xf[-1] == 1.0
+    assert np.allclose(xf[1:-1], (1 + g) / 2, rtol=0, atol=tol)
+
+
+@pytest.mark.parametrize("N", [2, 3, 4, 5, 6, 7, 8])
+def test_lagrange_operators_exact_on_polynomials(case_root, N):
+    o = oracle.Oracle(make_case(case_root, problem="orszag_tang", nx=2, ny=2, N=N, steps=1))
+    xs, xf = o.array("Xs"), o.array("Xf")
+    L = o.array("Lmat").reshape(N, N + 1).T  # L[ifp, is]
+    M = o.array("Mmat").reshape(N, N + 1).T  # M[ifp, is]
+    assert np.allclose(L.sum(axis=1), 1.0, atol=1e-13)
+    assert np.allclose(M.sum(axis=0), 0.0, atol=1e-11)
+    for k in range(N):
+        assert np.allclose(L @ xs ** k, xf ** k, atol=1e-12)
+    for k in range(N + 1):
+        dp = k * xs ** (k - 1) if k else np.zeros_like(xs)
+        assert np.allclose(M.T @ xf ** k, dp, atol=1e-10 * max(1, k * k))
+
+
+@pytest.mark.parametrize("N", [3, 4, 5])
+def test_free_stream_preservation(case_root, N):
+    """A constant state on curved cells gives resid = 0 to round-off."""
+    o = oracle.Oracle(make_case(case_root, problem="orszag_tang", nx=5, ny=4, N=N, jitter=0.15, seed=1, steps=1))
+    Q = o.array("Q")
+    q0 = np.array([1.3, 0.4, -0.2, 0.1, 5.0, 0.7, -0.3, 0.2, 0.0])
+    Q[:] = np.tile(q0, Q.size // 9)
+    o.compresid()
+    r = o.array("resid")
+    assert np.abs(r).max() < 1e-11
+
+
+def test_ct_keeps_divb_at_roundoff_on_affine_mesh(case_root):
+    o = oracle.Oracle(make_case(case_root, problem="orszag_tang", nx=8, ny=8, N=4, steps=1))
+    res, divb = o.step()
+    assert divb <= 1e-12
+    assert math.isfinite(res) and res > 0
+
+
+def test_orszag_tang_initial_data(case_root):
+    o = oracle.Oracle(make_case(case_root, problem="orszag_tang", nx=12, ny=12, N=4, jitter=0.1, seed=2, steps=1))
+    gam = o.getd("gam")
+    Q = o.array("Q").reshape(-1, 9)
+    xy = o.array("XXsolu").reshape(-1, 2)
+    x, y = xy[:, 0], xy[:, 1]
+    assert gam == 5.0 / 3
+    assert np.allclose(Q[:, 0], gam * gam, rtol=0, atol=0)
+    assert np.allclose(Q[:, 1], gam * gam * -np.sin(y), atol=1e-15)
+    assert np.allclose(Q[:, 2], gam * gam * np.sin(x), atol=1e-15)
+    assert np.allclose(Q[:, 8], 0.5 * np.cos(2 * x) + np.cos(y), atol=1e-15)
+    # B is the CT projection of the analytic field: close to (-sin y, sin 2x)
+    assert np.abs(Q[:, 5] + np.sin(y)).max() < 1e-2
+    assert np.abs(Q[:, 6] - np.sin(2 * x)).max() < 1e-2
+
+
+@pytest.mark.parametrize("nx,ny", [(2, 2), (3, 5), (8, 8)])
+def test_periodic_map_invariants(case_root, nx, ny):
+    o = oracle.Oracle(make_case(case_root, problem="orszag_tang", nx=nx, ny=ny, N=3, jitter=0.1, seed=1, steps=1))
+    nf, ni, npair = o.geti("NFACE"), o.geti("NINTER"), o.geti("NPAIR")
+    assert nf == 2 * nx * ny + nx + ny
+    assert ni == 2 * nx * ny - nx - ny
+    assert o.geti("NCYCL") == 2 * (nx + ny) and npair == nx + ny
+    IF2C = o.array("IF2C").reshape(4, nf).T
+    IC2F = o.array("IC2F").reshape(4, -1).T
+    for f in range(nf):
+        c1, c2, l1, l2 = IF2C[f]
+        assert IC2F[c1 - 1, l1 - 1] == f + 1
+        if c2:
+            assert IC2F[c2 - 1, l2 - 1] == f + 1
+    pairs = o.array("CYC2FPAIR").reshape(2, npair).T
+    assert len(set(pairs.ravel())) == 2 * npair
+
+
+def test_free_boundary_maps(case_root):
+    o = oracle.Oracle(make_case(case_root, problem="rotor", nx=6, ny=4, N=3, jitter=0.1, seed=1, steps=1))
+    assert o.geti("NFREE") == 2 * (6 + 4)
+    assert o.geti("NPAIR") == 0
+
+
+def test_restart_round_trip(case_root, tmp_path):
+    d = make_case(case_root, problem="orszag_tang", nx=4, ny=4, N=3, steps=1)
+    o = oracle.Oracle(d)
+    o.run(2)
+    p = str(tmp_path / "restart.dat")
+    assert o.write_restart(p) == 0
+    Q = o.array("Q").copy()
+    o2 = oracle.Oracle(d)
+    assert o2.read_restart(p) == 0
+    assert np.array_equal(o2.array("Q"), Q)
+    assert o2.geti("iter") == 2
+    raw = open(p, "rb").read()
+    assert len(raw) == 4 + 8 + 16 * (4 + 8 * 9 * 9)
