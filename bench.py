@@ -1,0 +1,349 @@
+"""Benchmark of the SD-MHD residual-and-time-step path on GB300.
+
+Workload (one "step" = one full time step of iterations.f90:19-87: five SSP-RK
+stages of compresid, the CT projection, and the norms every tenth step): the
+single-large-solve configuration -- Orszag-Tang on a periodic 512x512 quad mesh with
+interior nodes jittered by +-0.15h (seed 1), p = 4 (N = 5 solution points per
+direction), FP64, gamma = 5/3, Rusanov flux, AV on, RK_S5P3, dt from CFL 0.1.
+Synthetic seeded mesh in the reference's file formats (the reference ships none).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is DOF*RK-stage/s with the state resident on the
+device (CUDA events on the library's stream around K steps replayed from a CUDA
+graph); `e2e` is the same metric through the C-ABI with host buffers (each step:
+Q uploaded from pinned host memory, one step, Q downloaded).  `--impl reference`
+times the CPU oracle (a plain-C restatement of the reference; the Fortran reference
+cannot be built here) with every host thread on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "chorus-mhd_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+NX = 512
+N_SOL = 5
+JITTER = 0.15
+SEED = 1
+
+
+def workload_name():
+    return "orszag_tang_periodic_%dx%d_jitter%.2f_seed%d_p%d_N%d_fp64_rk_s5p3_av" % (NX, NX, JITTER, SEED, N_SOL - 1,
+                                                                                    N_SOL)
+
+METRIC = "DOF*RK-stage/s"
+HBM_FALLBACK = 6800.0
+FP64_PEAK_TFLOPS = 1.20  # measured DFMA microbenchmark on this machine's GB300 (600 G DFMA/s)
+
+
+def b_stage(N: int) -> float:
+    """Algorithmic bytes per element per RK stage (compulsory traffic with perfect
+    on-chip reuse): state r/w + RK register 216N^2, face traces 1728N, geometry and
+    neighbour ids 144, CT once per step (24N^2 + 64N)/5."""
+    return 216 * N * N + 1728 * N + 144 + (24 * N * N + 64 * N) / 5.0
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK, "fallback"
+
+
+def make_case(tmp):
+    from chorus_mhd import meshgen
+    spec = meshgen.CaseSpec(nx=NX, ny=NX, N=N_SOL, problem="orszag_tang", jitter=JITTER, seed=SEED, steps=200)
+    d = os.path.join(tmp, "case")
+    meshgen.write_case(spec, d)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                backend = "gloo"
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    from chorus_mhd import Mesh, Solver
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    tmp = tempfile.mkdtemp(prefix="chorus_bench_")
+    d = make_case(tmp)
+    mesh = Mesh(d)
+    sol = Solver(mesh, device=local)
+    N, nc = mesh.N, mesh.ncell
+    dof = nc * N * N
+    # warm-up (also builds the CUDA graphs)
+    sol.iterations(args.warmup)
+    stream = torch.cuda.ExternalStream(sol.stream_handle(), device=local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    per_step, per_diag = sol.launch_counts()
+    it0 = sol.iter
+    ndiag = sum(1 for i in range(it0 + 1, it0 + args.steps + 1) if i % 10 == 1)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        sol.iterations(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(world, ms)
+    launches = per_step * args.steps + per_diag * ndiag
+    value = world * dof * 5 * args.steps / (ms / 1e3)
+    Q = sol.state()
+    finite = bool(np.isfinite(Q).all())
+
+    # per-kernel stage profile (after the timed region; events around each kernel)
+    prof = sol.profile_stage(5)
+    names = ["e1_interp_inviscid_sensor", "f1_rusanov_faces", "e2_gradients", "f2_face_average_av",
+             "e3_viscous_divergence_rk"]
+    dom = max(range(5), key=lambda k: prof[k])
+    hbm_peak, peak_kind = measured_peaks()
+    stage_ms = prof[5]
+    achieved = b_stage(N) * nc / (stage_ms / 1e3) / 1e9
+    flops_es = FLOPS_PER_ELEMENT_STAGE.get(N)
+    fp64 = None
+    if flops_es:
+        tf = flops_es * nc / (stage_ms / 1e3) / 1e12
+        fp64 = {"achieved_tflops": tf, "peak_tflops": FP64_PEAK_TFLOPS, "frac": tf / FP64_PEAK_TFLOPS,
+                "flops_per_element_stage": flops_es, "source": "ncu sass op counts, profiles/"}
+
+    # end to end through the C-ABI with host buffers: H2D of Q, one step, D2H of Q
+    pinned = torch.empty(sol.nq, dtype=torch.float64, pin_memory=True)
+    qh = pinned.numpy()
+    qh[:] = Q
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sol.upload(qh)
+        sol.iterations(1)
+        out = sol.state()
+        qh[:] = out
+    t1 = time.perf_counter()
+    e2e_s = max_over_ranks(world, t1 - t0)
+    e2e = {"value": world * dof * 5 * e2e_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 8 * sol.nq,
+           "d2h_bytes_per_step": 8 * sol.nq, "steps": e2e_steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(d, dof)
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered %dx%d periodic mesh, Orszag-Tang initial data)" % (NX, NX),
+        "config": {"workload": workload_name(), "cells": nc, "N": N, "dof": dof, "stages_per_step": 5,
+                   "l2": "inputs larger than L2 (%.1f GB resident per replica)" % (sol.device_bytes() / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_STAGE.get(N),
+                     "kernel": "one RK stage (5 launches: %s)" % ", ".join(names),
+                     "algorithmic_bytes_per_element_stage": b_stage(N), "peak_kind": peak_kind,
+                     "stage_ms": stage_ms, "dominant_kernel": names[dom],
+                     "kernel_ms": dict(zip(names, prof[:5]))},
+        "fp64_pipe": fp64,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "state_finite": finite,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sol.close()
+    mesh.close()
+
+
+# FP64 flops per element per stage (2*DFMA + DADD + DMUL, from ncu SASS counters on
+# the stage kernels; see profiles/) and DRAM bytes per stage (ncu, scaled to 512^2)
+FLOPS_PER_ELEMENT_STAGE: dict = {}
+TRAFFIC_PER_STAGE: dict = {}
+
+
+def cpu_baseline(case_dir, dof, warm=1, timed=2):
+    """The oracle on the host cores, a bounded sample of the same workload."""
+    import oracle
+    threads = os.cpu_count() or 1
+    o = oracle.Oracle(case_dir, threads=threads)
+    for _ in range(warm):
+        o.step()
+    t0 = time.perf_counter()
+    for _ in range(timed):
+        o.step()
+    dt = time.perf_counter() - t0
+    v = dof * 5 * timed / dt
+    o.close()
+    return {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": "%d timed steps (after %d warm-up) of the same %dx%d N=%d solve, OpenMP over cells/faces"
+                      % (timed, warm, NX, NX, N_SOL), "seconds": dt}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    tmp = tempfile.mkdtemp(prefix="chorus_ref_")
+    d = make_case(tmp)
+    threads = os.cpu_count() or 1
+    o = oracle.Oracle(d, threads=threads)
+    nc = o.geti("NCELL")
+    N = o.geti("N")
+    dof = nc * N * N
+    # bounded sample: every warm-up/timed step is one full time step of the workload,
+    # capped so the whole run stays within a few minutes
+    t_est = None
+    for _ in range(args.warmup):
+        t0 = time.perf_counter()
+        o.step()
+        t_est = time.perf_counter() - t0
+    k = args.steps
+    if t_est and t_est * k > 150:
+        k = max(1, int(150 / t_est))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        o.step()
+    dt = time.perf_counter() - t0
+    v = dof * 5 * k / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world, "steps": k,
+            "warmup": args.warmup, "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded case)",
+            "config": {"workload": workload_name(), "cells": nc, "N": N, "dof": dof},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": "%d full time steps of the workload after %d warm-up (requested %d)"
+                                       % (k, args.warmup, args.steps)},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "plain-C restatement of the reference (the Fortran+MPI reference cannot be compiled: no "
+                    "Fortran compiler or MPI on the machines)"}
+    print(json.dumps(line), flush=True)
+    o.close()
+
+
+def main():
+    global NX, N_SOL
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="chorus", choices=["chorus", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nx", type=int, default=NX, help="cells per side (default: the 512x512 workload)")
+    ap.add_argument("--order-n", type=int, default=N_SOL, help="solution points per direction")
+    args = ap.parse_args()
+    NX, N_SOL = args.nx, args.order_n
+    if args.warmup < 3 and args.impl != "reference":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -54,6 +54,10 @@ SIGNATURES = {
     "getrusanovflux_gpu": (c_int, [c_int, c_double, dp, dp, dp, dp, dp, dp, ip, ip, dp]),
     "getifluxvectors_gpu": (c_int, [c_int, c_double, dp, dp, dp]),
     "getvfluxvectors_gpu": (c_int, [c_int, c_double, c_double, c_double, dp, dp, dp, dp]),
+    "chorus_gpu_stream": (c_void_p, [c_void_p]),
+    "chorus_gpu_profile_stage": (c_int, [c_void_p, c_int, dp]),
+    "chorus_gpu_launch_counts": (c_int, [c_void_p, ip, ip]),
+    "chorus_gpu_device_bytes": (ctypes.c_int64, [c_void_p]),
     "chorus_mesh_load": (c_int, [c_char_p, P(c_void_p)]),
     "chorus_mesh_free": (c_int, [c_void_p]),
     "chorus_mesh_info": (c_int, [c_void_p, P(ChorusDims), P(ChorusParams), ip, ip]),

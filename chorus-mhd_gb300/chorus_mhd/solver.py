@@ -164,6 +164,25 @@ class Solver:
         self.diagnostics.extend(out)
         return out
 
+    # ---- runtime helpers
+    def stream_handle(self) -> int:
+        """cudaStream_t of this solve (for events / ordering)."""
+        return int(self.L.chorus_gpu_stream(self._ctx) or 0)
+
+    def profile_stage(self, reps: int = 5) -> list:
+        """Mean durations (ms) of E1, F1, E2, F2, E3 and of a whole stage."""
+        ms = np.zeros(6)
+        check(self.L.chorus_gpu_profile_stage(self._ctx, int(reps), _dp(ms)))
+        return ms.tolist()
+
+    def launch_counts(self):
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        check(self.L.chorus_gpu_launch_counts(self._ctx, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def device_bytes(self) -> int:
+        return int(self.L.chorus_gpu_device_bytes(self._ctx))
+
     def write_restart(self, path: str):
         check(self.L.chorus_write_restart(self._ctx, path.encode(), self.iter, self.ctime))
 

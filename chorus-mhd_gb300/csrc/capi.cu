@@ -675,6 +675,57 @@ int iterations_gpu(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime, C
   return check_err_flag(c);
 }
 
+void* chorus_gpu_stream(ChorusCtx* c) { return c ? (void*)c->st : nullptr; }
+
+int64_t chorus_gpu_device_bytes(ChorusCtx* c) { return c ? (int64_t)c->arena_bytes : 0; }
+
+int chorus_gpu_launch_counts(ChorusCtx* c, int32_t* per_step, int32_t* per_diag) {
+  if (!c) return set_err(CHORUS_EINVAL, "null context");
+  const int nf = (c->nface2 + c->nface1) > 0 ? 1 : 0;
+  const int stage = 3 + 2 * nf;         // E1 E2 E3 (+ F1 F2)
+  const int ct = 2 + (c->nface2 > 0);   // element passes + face average
+  if (per_step) *per_step = 5 * stage + ct;
+  if (per_diag) *per_diag = 1 + nf + 4;  // E1, F1, nablaQsp, divB, reduce, record
+  return CHORUS_OK;
+}
+
+int chorus_gpu_profile_stage(ChorusCtx* c, int32_t reps, double* ms) {
+  if (!c || !ms || reps <= 0) return set_err(CHORUS_EINVAL, "bad argument");
+  if (ctx_device(c)) return CHORUS_ECUDA;
+  cudaEvent_t ev[6];
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  RKStage r = rk_blank();
+  r.cQ = 1.0;
+  r.cR = 0.377268915331368 * c->p.dt;
+  const SolveDev& s = c->sd;
+  for (int it = 0; it < reps; it++) {
+    CK(cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st));
+    CK(cudaEventRecord(ev[0], c->st));
+    c->D->e1(s, c->L[0], c->st);
+    CK(cudaEventRecord(ev[1], c->st));
+    c->D->f1(s, c->st);
+    CK(cudaEventRecord(ev[2], c->st));
+    c->D->e2(s, c->L[1], c->st);
+    CK(cudaEventRecord(ev[3], c->st));
+    c->D->f2(s, c->st);
+    CK(cudaEventRecord(ev[4], c->st));
+    c->D->e3(s, r, c->L[2], c->st);
+    CK(cudaEventRecord(ev[5], c->st));
+    CK(cudaEventSynchronize(ev[5]));
+    float t;
+    for (int k = 0; k < 5; k++) {
+      CK(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+      acc[k] += t;
+    }
+    CK(cudaEventElapsedTime(&t, ev[0], ev[5]));
+    acc[5] += t;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  for (int k = 0; k < 6; k++) ms[k] = acc[k] / reps;
+  return check_err_flag(c);
+}
+
 int chorus_gpu_get_eigvmax(ChorusCtx* c, double* eigvmax_g, double* epsilon0) {
   if (!c) return set_err(CHORUS_EINVAL, "null context");
   if (ctx_device(c)) return CHORUS_ECUDA;

@@ -145,6 +145,22 @@ int getvfluxvectors_gpu(int32_t n, double gam, double mu, double eta0, const dou
                         double* Gv /*n x 9*/);
 
 /* ------------------------------------------------------------------------------
+ * Runtime helpers (no reference counterpart)
+ * --------------------------------------------------------------------------- */
+/* The CUDA stream (cudaStream_t) all of ctx's work is enqueued on, so callers can
+ * record events on it or order their own work after it. */
+void* chorus_gpu_stream(ChorusCtx* ctx);
+/* Run `reps` RK stages (stage 1 of RK_S5P3, state updated) launching each stage
+ * kernel with CUDA events around it; ms[0..4] = mean duration of E1, F1, E2, F2, E3
+ * and ms[5] = mean duration of a whole stage. */
+int chorus_gpu_profile_stage(ChorusCtx* ctx, int32_t reps, double* ms);
+/* Kernel launches enqueued by one time step (5 stages + CT projection) and by the
+ * extra diagnostic of every tenth step. */
+int chorus_gpu_launch_counts(ChorusCtx* ctx, int32_t* per_step, int32_t* per_diag);
+/* Device bytes held by ctx (state, work arrays, geometry). */
+int64_t chorus_gpu_device_bytes(ChorusCtx* ctx);
+
+/* ------------------------------------------------------------------------------
  * Host-side setup for callers without the Fortran setup chain: reads QUAD.INP and
  * the .CEL/.VRT/.BND files and rebuilds the reference's maps (readinput.f90,
  * readGRIDinfo.f90, CHECK_MESH/CONNECTIVITY connectivity.f90, CONNECT_BDRY
