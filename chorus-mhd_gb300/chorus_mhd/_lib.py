@@ -52,6 +52,7 @@ SIGNATURES = {
     "fivestagerk_gpu": (c_int, [c_void_p, dp]),
     "iterations_gpu": (c_int, [c_void_p, c_int, ip, dp, P(ChorusDiag), c_int, ip]),
     "getrusanovflux_gpu": (c_int, [c_int, c_double, dp, dp, dp, dp, dp, dp, ip, ip, dp]),
+    "getrusanovflux_noalloc_gpu": (c_int, [c_int, c_double, dp, dp, dp, dp, dp, dp, ip, ip, dp]),
     "getifluxvectors_gpu": (c_int, [c_int, c_double, dp, dp, dp]),
     "getvfluxvectors_gpu": (c_int, [c_int, c_double, c_double, c_double, dp, dp, dp, dp]),
     "chorus_gpu_stream": (c_void_p, [c_void_p]),

@@ -143,6 +143,16 @@ int getifluxvectors_gpu(int32_t n, double gam, const double* Qi /*n x 8*/, doubl
 int getvfluxvectors_gpu(int32_t n, double gam, double mu, double eta0, const double* Qv /*n x 9*/,
                         const double* nablaQ /*n x 18, (9,2) per point*/, double* Fv /*n x 9*/,
                         double* Gv /*n x 9*/);
+/* getrusanovflux_gpu for callers that cannot allocate device memory (no counterpart in
+ * the reference): a host whose device memory is all held by its own pool, or one with
+ * work in flight that a cudaFree would stall.  Same arguments and results; the device
+ * staging lives in a fixed 10 MiB array inside the library, so n is limited to 32768
+ * points per call (larger n returns CHORUS_EINVAL) and no cudaMalloc/cudaFree is made.
+ * The first call on a device looks up the array's address (make it before any stream
+ * capture).  All calls share the array: calls that overlap on the GPU race. */
+int getrusanovflux_noalloc_gpu(int32_t n, double gam, const double* Qfl, const double* Qfr, double* Fnl,
+                               double* Fnr, double* Az, const double* normf, const int32_t* sign_l,
+                               const int32_t* sign_r, double* eigv);
 
 /* ------------------------------------------------------------------------------
  * Runtime helpers (no reference counterpart)
