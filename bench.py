@@ -196,6 +196,10 @@ def run_gpu(args):
     value = world * dof * 5 * args.steps / (ms / 1e3)
     Q = sol.state()
     finite = bool(np.isfinite(Q).all())
+    visc_frac = None
+    skip_active = bool(sol.get_option("skip_active"))
+    if skip_active:
+        visc_frac = float(sol.array("viscous_cells", nc).mean())
 
     # per-kernel stage profile (after the timed region; events around each kernel)
     prof = sol.profile_stage(5)
@@ -229,6 +233,15 @@ def run_gpu(args):
     e2e = {"value": world * dof * 5 * e2e_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 8 * sol.nq,
            "d2h_bytes_per_step": 8 * sol.nq, "steps": e2e_steps}
 
+    dev_bytes = sol.device_bytes()
+    sol.close()
+    mesh.close()
+    ens = None
+    if not args.no_ensemble:
+        ens = run_ensemble(args, local, tmp)
+    srv = None
+    if not args.no_serving:
+        srv = run_serving(args, local, tmp)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(d, dof)
@@ -238,7 +251,7 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered %dx%d periodic mesh, Orszag-Tang initial data)" % (NX, NX),
         "config": {"workload": workload_name(), "cells": nc, "N": N, "dof": dof, "stages_per_step": 5,
-                   "l2": "inputs larger than L2 (%.1f GB resident per replica)" % (sol.device_bytes() / 1e9),
+                   "l2": "inputs larger than L2 (%.1f GB resident per replica)" % (dev_bytes / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": e2e,
         "gpu_launches": launches,
@@ -252,11 +265,95 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "clocks": clocks,
         "state_finite": finite,
+        "viscous_work": {"skip_inactive_viscous": skip_active,
+                         "fraction_of_cells_with_viscous_flux": visc_frac},
+        "ensemble": ens,
+        "serving": srv,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    sol.close()
-    mesh.close()
+
+
+def run_ensemble(args, device, tmp):
+    """The batched configuration: 256 seeded solves of mixed size (32..256 cells per side,
+    log-uniform), order (N = 3..6) and problem, advanced as one batch and as the plain
+    per-solve loop (each solve's own CUDA-graph step, one solve after another)."""
+    import numpy as np
+    import torch
+    from chorus_mhd import Batch, Mesh, Solver, ensemble
+    specs = ensemble.draw(count=args.ensemble_count)
+    t0 = time.perf_counter()
+    dirs = ensemble.write_all(specs, os.path.join(tmp, "ensemble"))
+    solvers = []
+    for dd in dirs:
+        s = Solver(Mesh(dd), device=device)
+        s.set_option("diagnostics", 0)
+        solvers.append(s)
+    t_setup = time.perf_counter() - t0
+    dof = sum(s.ncell * s.N * s.N for s in solvers)
+    K = args.ensemble_steps
+    # plain loop: warm-up builds every solve's graph
+    for s in solvers:
+        s.iterations(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.iterations(K)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    b = Batch(device)
+    for s in solvers:
+        b.add(s)
+    b.step(1)
+    b.sync()
+    stream = torch.cuda.ExternalStream(b.stream_handle(), device=device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    b.step(K)
+    e1.record(stream)
+    b.sync()
+    t_batch = time.perf_counter() - t0
+    ms_batch = e0.elapsed_time(e1)
+    info = b.info()
+    finite = all(bool(np.isfinite(s.state()).all()) for s in solvers[:8])
+    b.close()
+    for s in solvers:
+        s.close()
+    Ns = {}
+    for s in solvers:
+        Ns[s.N] = Ns.get(s.N, 0) + 1
+    return {"solves": len(solvers), "dof": dof, "cells": sum(s.ncell for s in solvers), "steps": K,
+            "N_counts": {str(k): v for k, v in sorted(Ns.items())}, "setup_s": t_setup,
+            "batched": {"value": dof * 5 * K / (ms_batch / 1e3), "unit": METRIC, "ms_per_step": ms_batch / K,
+                        "wall_ms_per_step": t_batch * 1e3 / K, "cell_tiles": info["cell_tiles"],
+                        "face_tiles": info["face_tiles"]},
+            "plain_loop": {"value": dof * 5 * K / t_plain, "unit": METRIC, "ms_per_step": t_plain * 1e3 / K},
+            "batched_over_plain": (dof * 5 * K / (ms_batch / 1e3)) / (dof * 5 * K / t_plain),
+            "spot_check_finite": finite,
+            "draw": "ensemble.draw(count=%d, lo=32, hi=256, seed=2024): rotor side >= ceil(192/N)"
+                    % args.ensemble_count}
+
+
+def run_serving(args, device, tmp):
+    """Poisson request streams (end times U(0.1, 1.0)) over a pool of small mixed solves,
+    served with continuous batching under a 120 GB budget and by the plain sequential
+    loop; p50/p99 time-to-solution and throughput per arrival rate."""
+    from chorus_mhd import serve
+    dirs = serve.serving_cases(os.path.join(tmp, "serving"))
+    out = {"pool": "ensemble.draw(count=24, lo=16, hi=32, seed=11, problems=(orszag_tang, alfven))",
+           "hbm_budget_bytes": 120 * 10 ** 9, "requests_per_rate": args.serving_requests, "rates": {}}
+    serve.serve([(dirs[0], 0.0, 0.01)], mode="batched")  # warm-up
+    for rate in args.serving_rates:
+        reqs = serve.poisson_requests(rate, args.serving_requests, dirs, seed=int(rate))
+        rb, mb = serve.serve(reqs, mode="batched", hbm_budget_bytes=120 * 10 ** 9, device=device)
+        rs, ms = serve.serve(reqs, mode="sequential", device=device)
+        b, q = serve.summarize(rb, mb), serve.summarize(rs, ms)
+        out["rates"][str(rate)] = {"batched": b, "sequential": q,
+                                   "throughput_ratio": b["throughput_dof_stage_per_s"] / max(q["throughput_dof_stage_per_s"], 1e-30),
+                                   "p99_ratio_sequential_over_batched": q["p99_latency_s"] / max(b["p99_latency_s"], 1e-30)}
+    return out
 
 
 # FP64 flops per element per stage (2*DFMA + DADD + DMUL, from ncu SASS counters on
@@ -333,6 +430,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="chorus", choices=["chorus", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--ensemble-count", type=int, default=256)
+    ap.add_argument("--ensemble-steps", type=int, default=3)
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-requests", type=int, default=24)
+    ap.add_argument("--serving-rates", type=float, nargs="+", default=[10.0, 100.0, 500.0])
     ap.add_argument("--nx", type=int, default=NX, help="cells per side (default: the 512x512 workload)")
     ap.add_argument("--order-n", type=int, default=N_SOL, help="solution points per direction")
     args = ap.parse_args()

@@ -27,6 +27,20 @@ class ChorusParams(ctypes.Structure):
                 ("NCELLGLOB", c_int), ("vismode", c_int), ("ARTIV", c_int), ("k_stage", c_int)]
 
 
+class ChorusServeRequest(ctypes.Structure):
+    _fields_ = [("case_dir", c_char_p), ("arrival_s", c_double), ("end_time", c_double)]
+
+
+class ChorusServeConfig(ctypes.Structure):
+    _fields_ = [("device", c_int), ("mode", c_int), ("hbm_budget_bytes", ctypes.c_int64), ("max_active", c_int),
+                ("pad", c_int)]
+
+
+class ChorusServeResult(ctypes.Structure):
+    _fields_ = [("admit_s", c_double), ("finish_s", c_double), ("latency_s", c_double), ("dof", ctypes.c_int64),
+                ("steps", c_int), ("status", c_int)]
+
+
 class ChorusDiag(ctypes.Structure):
     _fields_ = [("iter", c_int), ("pad", c_int), ("ctime", c_double), ("residglob", c_double),
                 ("divBglob", c_double), ("eigvmax_g", c_double), ("epsilon0", c_double)]
@@ -56,9 +70,21 @@ SIGNATURES = {
     "getifluxvectors_gpu": (c_int, [c_int, c_double, dp, dp, dp]),
     "getvfluxvectors_gpu": (c_int, [c_int, c_double, c_double, c_double, dp, dp, dp, dp]),
     "chorus_gpu_stream": (c_void_p, [c_void_p]),
+    "chorus_gpu_set_option": (c_int, [c_void_p, c_char_p, ctypes.c_int64]),
+    "chorus_gpu_get_option": (ctypes.c_int64, [c_void_p, c_char_p]),
     "chorus_gpu_profile_stage": (c_int, [c_void_p, c_int, dp]),
     "chorus_gpu_launch_counts": (c_int, [c_void_p, ip, ip]),
     "chorus_gpu_device_bytes": (ctypes.c_int64, [c_void_p]),
+    "chorus_batch_create": (c_int, [c_int, P(c_void_p)]),
+    "chorus_batch_free": (c_int, [c_void_p]),
+    "chorus_batch_add": (c_int, [c_void_p, c_void_p, ip]),
+    "chorus_batch_remove": (c_int, [c_void_p, c_int]),
+    "chorus_batch_step": (c_int, [c_void_p, c_int]),
+    "chorus_batch_sync": (c_int, [c_void_p, ip]),
+    "chorus_batch_stream": (c_int, [c_void_p, P(c_void_p)]),
+    "chorus_batch_info": (c_int, [c_void_p, ip, ip, ip, P(ctypes.c_int64)]),
+    "chorus_serve_run": (c_int, [P(ChorusServeRequest), c_int, P(ChorusServeConfig), P(ChorusServeResult), dp]),
+    "chorus_mesh_device_bytes": (ctypes.c_int64, [c_void_p]),
     "chorus_mesh_load": (c_int, [c_char_p, P(c_void_p)]),
     "chorus_mesh_free": (c_int, [c_void_p]),
     "chorus_mesh_info": (c_int, [c_void_p, P(ChorusDims), P(ChorusParams), ip, ip]),

@@ -165,6 +165,12 @@ class Solver:
         return out
 
     # ---- runtime helpers
+    def set_option(self, name: str, value: int):
+        check(self.L.chorus_gpu_set_option(self._ctx, name.encode(), int(value)))
+
+    def get_option(self, name: str) -> int:
+        return int(self.L.chorus_gpu_get_option(self._ctx, name.encode()))
+
     def stream_handle(self) -> int:
         """cudaStream_t of this solve (for events / ordering)."""
         return int(self.L.chorus_gpu_stream(self._ctx) or 0)

@@ -1,0 +1,510 @@
+// batch.cu -- many independent solves of mixed size and order advanced together:
+// one launch per pass for the whole ensemble.
+//
+// Each pass is a persistent kernel (a fixed grid of CTAs sized to the GPU) that pulls
+// tiles from a device work table with an atomic counter.  A cell tile is
+// (solve, first cell, cells, N), a face tile (solve, first face point, points, N); the
+// kernel copies the tile's solve descriptor to shared memory and runs the same
+// per-N pass body as the single-solve kernels, so a solve gives the same bits alone and
+// in a batch.  Tables, counts and per-solve RK coefficients live in device memory and
+// are rewritten between steps, so one captured CUDA graph serves any composition that
+// fits the table capacities (the serving loop changes the mix every step).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "chorus_internal.h"
+#include "kernels.cuh"
+
+namespace chorus {
+
+int set_err(int code, const char* fmt, ...);
+
+static __constant__ OpsN c_ops_all[kMaxN + 1];
+
+template <int N>
+struct OpsAll {
+  __device__ static const OpsN& ops() { return c_ops_all[N]; }
+};
+
+void upload_ops_all(int N, const OpsN& o) {
+  cudaMemcpyToSymbol(c_ops_all, &o, sizeof(OpsN), sizeof(OpsN) * N);
+}
+
+struct BatchDev {
+  const SolveDev* solves;   // per slot (eig/err point into the batch's own arrays)
+  const int4* ctiles;       // (slot, e0, cnt, N)
+  const int4* ftiles;       // (slot, t0, cnt, N)
+  const int* ntiles;        // [0] cell tiles, [1] face tiles
+  int* counters;            // per-launch tile counters, zeroed at the start of each stage
+  const RKStage* rk;        // [5][cap]
+  int cap;
+  int pad;
+};
+
+namespace {
+
+__device__ __forceinline__ int next_tile(int* counter) {
+  __shared__ int t;
+  __syncthreads();
+  if (threadIdx.x == 0) t = atomicAdd(counter, 1);
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ const SolveDev& load_solve(const SolveDev* src) {
+  __shared__ __align__(16) SolveDev ss;
+  constexpr int n4 = sizeof(SolveDev) / 16;
+  static_assert(sizeof(SolveDev) % 16 == 0, "SolveDev must be a multiple of 16 bytes");
+  const int4* a = reinterpret_cast<const int4*>(src);
+  int4* d = reinterpret_cast<int4*>(&ss);
+  for (int i = threadIdx.x; i < n4; i += blockDim.x) d[i] = a[i];
+  __syncthreads();
+  return ss;
+}
+
+#define CHORUS_BATCH_SWITCH(NV, CALL) \
+  switch (NV) {                       \
+    case 2: CALL(2); break;           \
+    case 3: CALL(3); break;           \
+    case 4: CALL(4); break;           \
+    case 5: CALL(5); break;           \
+    case 6: CALL(6); break;           \
+    case 7: CALL(7); break;           \
+    case 8: CALL(8); break;           \
+    default: break;                   \
+  }
+
+__global__ void __launch_bounds__(128) kb_e1(BatchDev b, int slot, int sensor_on) {
+  extern __shared__ double sm[];
+  const int nt = b.ntiles[0];
+  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
+    const int4 T = b.ctiles[ti];
+    const SolveDev& s = load_solve(b.solves + T.x);
+    const int sensor = sensor_on ? s.artiv : 0;
+#define CALL(n) e1_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sensor, sm)
+    CHORUS_BATCH_SWITCH(T.w, CALL)
+#undef CALL
+  }
+}
+
+__global__ void __launch_bounds__(128) kb_e2(BatchDev b, int slot) {
+  extern __shared__ double sm[];
+  const int nt = b.ntiles[0];
+  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
+    const int4 T = b.ctiles[ti];
+    const SolveDev& s = load_solve(b.solves + T.x);
+#define CALL(n) e2_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sm)
+    CHORUS_BATCH_SWITCH(T.w, CALL)
+#undef CALL
+  }
+}
+
+__global__ void __launch_bounds__(128) kb_e3(BatchDev b, int slot, int stage) {
+  extern __shared__ double sm[];
+  const int nt = b.ntiles[0];
+  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
+    const int4 T = b.ctiles[ti];
+    const SolveDev& s = load_solve(b.solves + T.x);
+    const RKStage& rk = b.rk[stage * b.cap + T.x];
+#define CALL(n) e3_body<n, OpsAll<n>>(s, T.y, T.z, T.z, rk, 1, sm)
+    CHORUS_BATCH_SWITCH(T.w, CALL)
+#undef CALL
+  }
+}
+
+__global__ void __launch_bounds__(128) kb_ct(BatchDev b, int slot, int mode) {
+  extern __shared__ double sm[];
+  const int nt = b.ntiles[0];
+  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
+    const int4 T = b.ctiles[ti];
+    const SolveDev& s = load_solve(b.solves + T.x);
+#define CALL(n) ct_elem_body<n, OpsAll<n>>(s, T.y, T.z, T.z, mode, sm)
+    CHORUS_BATCH_SWITCH(T.w, CALL)
+#undef CALL
+  }
+}
+
+// face passes: which = 0 Rusanov (F1), 1 gradient/AV averages (F2), 2 CT average
+__global__ void __launch_bounds__(128) kb_face(BatchDev b, int slot, int which) {
+  const int nt = b.ntiles[1];
+  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
+    const int4 T = b.ftiles[ti];
+    const SolveDev& s = load_solve(b.solves + T.x);
+    const int t = T.y + threadIdx.x;
+    const bool in = threadIdx.x < T.z;
+    if (which == 0) {
+      unsigned long long evb = 0ull;
+      if (in) {
+#define CALL(n) evb = f1_point<n>(s, t)
+        CHORUS_BATCH_SWITCH(T.w, CALL)
+#undef CALL
+      }
+      block_max_ull(evb, s.eig);
+    } else if (in) {
+      if (which == 1) {
+#define CALL(n) f2_point<n>(s, t)
+        CHORUS_BATCH_SWITCH(T.w, CALL)
+#undef CALL
+      } else {
+#define CALL(n) ctface_point<n>(s, t)
+        CHORUS_BATCH_SWITCH(T.w, CALL)
+#undef CALL
+      }
+    }
+  }
+}
+
+size_t cell_smem_bytes(int N, int epb) {
+  const int NS = N * N, NFP = 2 * (N + 1) * N;
+  size_t e1 = (size_t)epb * (NS * 9 + 2 * NS);
+  size_t e2 = (size_t)epb * (NFP * 9 + NFP + NS * 16);
+  size_t e3 = (size_t)epb * (NFP * 8 + NS);
+  size_t ct = (size_t)epb * NFP;
+  return sizeof(double) * std::max(std::max(e1, e2), std::max(e3, ct));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct BatchSlot {
+  ChorusCtx* ctx = nullptr;
+  SolveDev sd{};
+  int N = 0, NC = 0, nfp_faces = 0;
+  int epb = 4;
+  double dt = 0.0;
+  int k_stage = 3;
+  int64_t steps = 0;
+  bool active = false;
+};
+
+}  // namespace chorus
+
+using namespace chorus;
+
+// accessors of ChorusCtx implemented in capi.cu
+namespace chorus {
+const SolveDev& ctx_solve(const ChorusCtx* c);
+int ctx_device_of(const ChorusCtx* c);
+double ctx_dt(const ChorusCtx* c);
+int ctx_kstage(const ChorusCtx* c);
+int ctx_epb(const ChorusCtx* c, int pass);
+void ensure_ops_all(int dev, int N, const ChorusCtx* c);
+}  // namespace chorus
+
+struct ChorusBatch {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  int cap_solves = 0, cap_ctiles = 0, cap_ftiles = 0;
+  std::vector<BatchSlot> slots;
+  // device tables
+  SolveDev* d_solves = nullptr;
+  int4* d_ctiles = nullptr;
+  int4* d_ftiles = nullptr;
+  int* d_ntiles = nullptr;
+  int* d_counters = nullptr;
+  RKStage* d_rk = nullptr;
+  unsigned long long* d_eig = nullptr;
+  unsigned int* d_err = nullptr;
+  int grid_cells = 0, grid_faces = 0;
+  size_t smem = 0;
+  bool dirty = true;
+  cudaGraphExec_t graph = nullptr;
+  size_t graph_smem = 0;
+  int ctiles = 0, ftiles = 0;
+};
+
+static constexpr int kCounterSlots = 16;
+
+static int batch_alloc(ChorusBatch* b, int cap_solves, int cap_ctiles, int cap_ftiles) {
+  auto fr = [](void* p) { if (p) cudaFree(p); };
+  fr(b->d_solves); fr(b->d_ctiles); fr(b->d_ftiles); fr(b->d_rk); fr(b->d_eig); fr(b->d_err);
+  b->d_solves = nullptr; b->d_ctiles = nullptr; b->d_ftiles = nullptr; b->d_rk = nullptr;
+  b->d_eig = nullptr; b->d_err = nullptr;
+  cudaError_t e = cudaMalloc(&b->d_solves, sizeof(SolveDev) * std::max(cap_solves, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_ctiles, sizeof(int4) * std::max(cap_ctiles, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_ftiles, sizeof(int4) * std::max(cap_ftiles, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_rk, sizeof(RKStage) * 5 * std::max(cap_solves, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_eig, sizeof(unsigned long long) * 2 * std::max(cap_solves, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(unsigned int) * std::max(cap_solves, 1));
+  if (e != cudaSuccess) return set_err(CHORUS_ENOMEM, "batch tables: %s", cudaGetErrorString(e));
+  cudaMemsetAsync(b->d_err, 0, sizeof(unsigned int) * std::max(cap_solves, 1), b->st);
+  b->cap_solves = cap_solves;
+  b->cap_ctiles = cap_ctiles;
+  b->cap_ftiles = cap_ftiles;
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  return CHORUS_OK;
+}
+
+// RK stage records of one solve (same coefficients as the single-solve path)
+static void rk_records(const SolveDev& s, double dt, int k_stage, RKStage* r) {
+  for (int k = 0; k < 5; k++) std::memset(&r[k], 0, sizeof(RKStage));
+  if (k_stage == 5) {
+    const double a11 = 0.39175222700392, a21 = 0.44437049406734, a22 = 0.55562950593266, a23 = 0.36841059262959,
+                 a31 = 0.6201018513854, a32 = 0.3798981486146, a33 = 0.25189177424738, a41 = 0.17807995410773,
+                 a42 = 0.82192004589227, a43 = 0.54497475021237, a51 = 0.00683325884039, a52 = 0.51723167208978,
+                 a53 = 0.12759831133288, a54 = 0.34833675773694, a55 = 0.08460416338212, a56 = 0.22600748319395;
+    r[0].cQ = 1.0; r[0].cR = dt * a11; r[0].save_old = s.Qk0;
+    r[1].nsrc = 1; r[1].src[0] = s.Qk0; r[1].c[0] = a21; r[1].cQ = a22; r[1].cR = a23 * dt; r[1].save_new = s.Qr2;
+    r[2].nsrc = 1; r[2].src[0] = s.Qk0; r[2].c[0] = a31; r[2].cQ = a32; r[2].cR = a33 * dt; r[2].save_new = s.Qr3;
+    r[3].nsrc = 1; r[3].src[0] = s.Qk0; r[3].c[0] = a41; r[3].cQ = a42; r[3].cR = a43 * dt; r[3].save_R = s.R0;
+    r[4].nsrc = 3; r[4].src[0] = s.Qk0; r[4].src[1] = s.Qr2; r[4].src[2] = s.Qr3;
+    r[4].c[0] = a51; r[4].c[1] = a52; r[4].c[2] = a53; r[4].cQ = a54; r[4].cR = a56 * dt;
+    r[4].R0 = s.R0; r[4].cR0 = a55 * dt;
+  } else {
+    const double a30 = 0.355909775063327, a32 = 0.644090224936674, a40 = 0.367933791638137,
+                 a43 = 0.632066208361863, a52 = 0.237593836598569, a54 = 0.762406163401431,
+                 b10 = 0.377268915331368, b21 = 0.377268915331368, b32 = 0.242995220537396,
+                 b43 = 0.238458932846290, b54 = 0.287632146308408;
+    r[0].cQ = 1.0; r[0].cR = b10 * dt; r[0].save_old = s.Qk0;
+    r[1].cQ = 1.0; r[1].cR = b21 * dt; r[1].save_new = s.Qka;
+    r[2].nsrc = 1; r[2].src[0] = s.Qk0; r[2].c[0] = a30; r[2].cQ = a32; r[2].cR = b32 * dt;
+    r[3].nsrc = 1; r[3].src[0] = s.Qk0; r[3].c[0] = a40; r[3].cQ = a43; r[3].cR = b43 * dt;
+    r[4].nsrc = 1; r[4].src[0] = s.Qka; r[4].c[0] = a52; r[4].cQ = a54; r[4].cR = b54 * dt;
+  }
+  r[4].write_resid = 1;
+}
+
+static int batch_rebuild(ChorusBatch* b) {
+  std::vector<int> act;
+  for (int i = 0; i < (int)b->slots.size(); i++)
+    if (b->slots[i].active) act.push_back(i);
+  // tiles: largest N first so the slowest tiles start early
+  std::vector<int4> ct, ft;
+  std::vector<int> order(act);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->slots[a].N > b->slots[c].N; });
+  size_t smem = 0;
+  for (int i : order) {
+    const BatchSlot& sl = b->slots[i];
+    for (int e0 = 0; e0 < sl.NC; e0 += sl.epb) ct.push_back(make_int4(i, e0, std::min(sl.epb, sl.NC - e0), sl.N));
+    for (int t0 = 0; t0 < sl.nfp_faces; t0 += 128) ft.push_back(make_int4(i, t0, std::min(128, sl.nfp_faces - t0), sl.N));
+    smem = std::max(smem, cell_smem_bytes(sl.N, sl.epb));
+  }
+  const int ns = (int)b->slots.size();
+  if (ns > b->cap_solves || (int)ct.size() > b->cap_ctiles || (int)ft.size() > b->cap_ftiles) {
+    int rc = batch_alloc(b, std::max(ns * 2, 16), std::max((int)ct.size() * 2, 1024), std::max((int)ft.size() * 2, 1024));
+    if (rc) return rc;
+  }
+  std::vector<SolveDev> sd(ns);
+  std::vector<RKStage> rk((size_t)5 * b->cap_solves);
+  for (int i = 0; i < ns; i++) {
+    sd[i] = b->slots[i].sd;
+    sd[i].eig = b->d_eig + 2 * i;
+    sd[i].err = b->d_err + i;
+    RKStage r[5];
+    rk_records(sd[i], b->slots[i].dt, b->slots[i].k_stage, r);
+    for (int k = 0; k < 5; k++) rk[(size_t)k * b->cap_solves + i] = r[k];
+  }
+  cudaError_t e = cudaSuccess;
+  if (ns) e = cudaMemcpyAsync(b->d_solves, sd.data(), sizeof(SolveDev) * ns, cudaMemcpyHostToDevice, b->st);
+  if (e == cudaSuccess && !ct.empty())
+    e = cudaMemcpyAsync(b->d_ctiles, ct.data(), sizeof(int4) * ct.size(), cudaMemcpyHostToDevice, b->st);
+  if (e == cudaSuccess && !ft.empty())
+    e = cudaMemcpyAsync(b->d_ftiles, ft.data(), sizeof(int4) * ft.size(), cudaMemcpyHostToDevice, b->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_rk, rk.data(), sizeof(RKStage) * rk.size(), cudaMemcpyHostToDevice, b->st);
+  int nt[2] = {(int)ct.size(), (int)ft.size()};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_ntiles, nt, sizeof nt, cudaMemcpyHostToDevice, b->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+  if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch tables upload: %s", cudaGetErrorString(e));
+  b->ctiles = nt[0];
+  b->ftiles = nt[1];
+  if (smem > b->graph_smem && b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  b->smem = std::max(b->smem, smem);
+  b->dirty = false;
+  return CHORUS_OK;
+}
+
+static void batch_enqueue_step(ChorusBatch* b) {
+  BatchDev a;
+  a.solves = b->d_solves;
+  a.ctiles = b->d_ctiles;
+  a.ftiles = b->d_ftiles;
+  a.ntiles = b->d_ntiles;
+  a.counters = b->d_counters;
+  a.rk = b->d_rk;
+  a.cap = b->cap_solves;
+  a.pad = 0;
+  const size_t sm = b->smem;
+  for (int stage = 0; stage < 5; stage++) {
+    cudaMemsetAsync(b->d_counters, 0, sizeof(int) * kCounterSlots, b->st);
+    cudaMemsetAsync(b->d_eig, 0, sizeof(unsigned long long) * 2 * b->cap_solves, b->st);
+    kb_e1<<<b->grid_cells, 128, sm, b->st>>>(a, 0, 1);
+    kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 1, 0);
+    kb_e2<<<b->grid_cells, 128, sm, b->st>>>(a, 2);
+    kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 3, 1);
+    kb_e3<<<b->grid_cells, 128, sm, b->st>>>(a, 4, stage);
+  }
+  cudaMemsetAsync(b->d_counters, 0, sizeof(int) * kCounterSlots, b->st);
+  kb_ct<<<b->grid_cells, 128, sm, b->st>>>(a, 5, 0);
+  kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 6, 2);
+  kb_ct<<<b->grid_cells, 128, sm, b->st>>>(a, 7, 2);
+}
+
+extern "C" {
+
+int chorus_batch_create(int32_t device, ChorusBatch** out) {
+  if (!out) return set_err(CHORUS_EINVAL, "null argument");
+  *out = nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) return set_err(CHORUS_ECUDA, "cudaSetDevice(%d)", device);
+  ChorusBatch* b = new ChorusBatch();
+  b->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_ntiles, sizeof(int) * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_counters, sizeof(int) * kCounterSlots);
+  if (e != cudaSuccess) {
+    delete b;
+    return set_err(CHORUS_ECUDA, "batch create: %s", cudaGetErrorString(e));
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  b->grid_cells = sms * 8;  // persistent CTAs: 8 per SM (occupancy is not what bounds FP64)
+  b->grid_faces = sms * 8;
+  const int lim = 200 * 1024;
+  cudaFuncSetAttribute(kb_e1, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(kb_e2, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(kb_e3, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(kb_ct, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  int rc = batch_alloc(b, 16, 4096, 4096);
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return CHORUS_OK;
+}
+
+int chorus_batch_free(ChorusBatch* b) {
+  if (!b) return CHORUS_OK;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->st);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  void* ptrs[] = {b->d_solves, b->d_ctiles, b->d_ftiles, b->d_ntiles, b->d_counters, b->d_rk, b->d_eig, b->d_err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  cudaStreamDestroy(b->st);
+  delete b;
+  return CHORUS_OK;
+}
+
+int chorus_batch_add(ChorusBatch* b, ChorusCtx* ctx, int32_t* slot) {
+  if (!b || !ctx) return set_err(CHORUS_EINVAL, "null argument");
+  if (ctx_device_of(ctx) != b->device) return set_err(CHORUS_EINVAL, "context and batch are on different devices");
+  BatchSlot sl;
+  sl.ctx = ctx;
+  sl.sd = ctx_solve(ctx);
+  sl.N = sl.sd.N;
+  sl.NC = sl.sd.NC;
+  sl.nfp_faces = (sl.sd.nface2 + sl.sd.nface1) * sl.N;
+  sl.epb = std::max(1, std::min(ctx_epb(ctx, 2), 64));
+  sl.dt = ctx_dt(ctx);
+  sl.k_stage = ctx_kstage(ctx);
+  sl.active = true;
+  ensure_ops_all(b->device, sl.N, ctx);
+  int idx = -1;
+  for (int i = 0; i < (int)b->slots.size(); i++)
+    if (!b->slots[i].ctx) { idx = i; break; }
+  if (idx < 0) {
+    idx = (int)b->slots.size();
+    b->slots.push_back(sl);
+  } else {
+    b->slots[idx] = sl;
+  }
+  b->dirty = true;
+  if (slot) *slot = idx;
+  return CHORUS_OK;
+}
+
+int chorus_batch_remove(ChorusBatch* b, int32_t slot) {
+  if (!b || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].ctx)
+    return set_err(CHORUS_EINVAL, "bad batch slot %d", slot);
+  cudaStreamSynchronize(b->st);
+  b->slots[slot] = BatchSlot();
+  b->dirty = true;
+  return CHORUS_OK;
+}
+
+int chorus_batch_step(ChorusBatch* b, int32_t nsteps) {
+  if (!b || nsteps < 0) return set_err(CHORUS_EINVAL, "bad argument");
+  if (cudaSetDevice(b->device) != cudaSuccess) return set_err(CHORUS_ECUDA, "cudaSetDevice");
+  if (b->dirty) {
+    int rc = batch_rebuild(b);
+    if (rc) return rc;
+  }
+  if (b->ctiles == 0) return CHORUS_OK;
+  if (!b->graph) {
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "capture: %s", cudaGetErrorString(e));
+    batch_enqueue_step(b);
+    e = cudaStreamEndCapture(b->st, &g);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+    if (e == cudaSuccess) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch graph: %s", cudaGetErrorString(e));
+    b->graph_smem = b->smem;
+  }
+  for (int s = 0; s < nsteps; s++) {
+    cudaError_t e = cudaGraphLaunch(b->graph, b->st);
+    if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch step: %s", cudaGetErrorString(e));
+  }
+  for (auto& sl : b->slots)
+    if (sl.ctx && sl.active) sl.steps += nsteps;
+  return CHORUS_OK;
+}
+
+int chorus_batch_sync(ChorusBatch* b, int32_t* err_slot) {
+  if (!b) return set_err(CHORUS_EINVAL, "null batch");
+  cudaError_t e = cudaStreamSynchronize(b->st);
+  if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch sync: %s", cudaGetErrorString(e));
+  const int ns = (int)b->slots.size();
+  if (err_slot) *err_slot = -1;
+  if (ns) {
+    std::vector<unsigned int> h(ns);
+    e = cudaMemcpy(h.data(), b->d_err, sizeof(unsigned int) * ns, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch err read: %s", cudaGetErrorString(e));
+    for (int i = 0; i < ns; i++)
+      if (h[i] && b->slots[i].ctx) {
+        if (err_slot) *err_slot = i;
+        return set_err(CHORUS_ESTATE, "solve in batch slot %d flagged a non-finite wave speed", i);
+      }
+  }
+  return CHORUS_OK;
+}
+
+int chorus_batch_stream(ChorusBatch* b, void** stream) {
+  if (!b || !stream) return set_err(CHORUS_EINVAL, "null argument");
+  *stream = (void*)b->st;
+  return CHORUS_OK;
+}
+
+int chorus_batch_info(ChorusBatch* b, int32_t* n_solves, int32_t* cell_tiles, int32_t* face_tiles, int64_t* dofs) {
+  if (!b) return set_err(CHORUS_EINVAL, "null batch");
+  if (b->dirty) {
+    int rc = batch_rebuild(b);
+    if (rc) return rc;
+  }
+  int n = 0;
+  int64_t d = 0;
+  for (auto& sl : b->slots)
+    if (sl.ctx && sl.active) {
+      n++;
+      d += (int64_t)sl.NC * sl.N * sl.N;
+    }
+  if (n_solves) *n_solves = n;
+  if (cell_tiles) *cell_tiles = b->ctiles;
+  if (face_tiles) *face_tiles = b->ftiles;
+  if (dofs) *dofs = d;
+  return CHORUS_OK;
+}
+
+}  // extern "C"

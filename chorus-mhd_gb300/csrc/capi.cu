@@ -148,7 +148,28 @@ struct ChorusCtx {
   double graph_dt = NAN;
   int graph_k = -1;
   const Dispatch* D = nullptr;
+  int skip_option = 1;  // skip viscous work where it is exactly zero (mu = eta0 = 0, no AV)
+  int diagnostics = 1;  // norms every tenth step in iterations_gpu
+  std::vector<double> Lmat, Mmat, Xs, Xf;
 };
+
+namespace chorus {
+void upload_ops_all(int N, const OpsN& o);
+const SolveDev& ctx_solve(const ChorusCtx* c) { return c->sd; }
+int ctx_device_of(const ChorusCtx* c) { return c->device; }
+double ctx_dt(const ChorusCtx* c) { return c->p.dt; }
+int ctx_kstage(const ChorusCtx* c) { return c->p.k_stage; }
+int ctx_epb(const ChorusCtx* c, int pass) { return c->L[pass].epb; }
+static bool g_ops_all_done[64][kMaxN + 1];
+void ensure_ops_all(int dev, int N, const ChorusCtx* c) {
+  std::lock_guard<std::mutex> lk(g_ops_mu);
+  if (dev >= 0 && dev < 64 && g_ops_all_done[dev][N]) return;
+  OpsN o;
+  make_ops(N, c->Lmat.data(), c->Mmat.data(), c->Xs.data(), c->Xf.data(), o);
+  upload_ops_all(N, o);
+  if (dev >= 0 && dev < 64) g_ops_all_done[dev][N] = true;
+}
+}  // namespace chorus
 
 static int ctx_device(ChorusCtx* c) {
   CK(cudaSetDevice(c->device));
@@ -164,6 +185,23 @@ struct ArenaPlan {
     return o;
   }
 };
+
+// bytes of one solve's device arena (the same allocation sequence as chorus_gpu_bind)
+static size_t arena_plan_bytes(int N, int NC, int nface2, int nface1, int k_stage) {
+  const int NS = N * N, NFP = 2 * (N + 1) * N, NG = 4 * (N + 1);
+  const size_t nq = (size_t)NC * NS * 9, nfp = (size_t)NC * NFP;
+  ArenaPlan P;
+  P.take<double>(nq); P.take<double>(nq); P.take<double>(nq);
+  if (k_stage == 5) { P.take<double>(nq); P.take<double>(nq); P.take<double>(nq); }
+  P.take<double>(nq); P.take<double>(nfp * 9); P.take<double>(nfp * 8); P.take<double>(nfp);
+  P.take<double>((size_t)NC * NS * 18); P.take<double>(nfp * 18); P.take<double>((size_t)NC * NS * 2);
+  P.take<double>(nfp * 2); P.take<double>((size_t)NC * NS * NG); P.take<double>((size_t)NC * NS);
+  P.take<double>(NC); P.take<double>((size_t)NC * 4); P.take<double>((size_t)NC * 2);
+  P.take<int4>(nface2 + 1); P.take<int2>(nface1 + 1); P.take<FaceNorm>((size_t)nface2 * N + 1);
+  P.take<FaceNorm>((size_t)nface1 * N + 1); P.take<unsigned long long>(4); P.take<unsigned int>(4);
+  P.take<double>(8); P.take<int>(NC); P.take<int>(NC); P.take<int4>(NC);
+  return P.off;
+}
 
 extern "C" {
 
@@ -202,6 +240,10 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   c->device = device;
   c->dims = *dims;
   c->p = *params;
+  c->Lmat.assign(Lmat, Lmat + (N + 1) * N);
+  c->Mmat.assign(Mmat, Mmat + (N + 1) * N);
+  c->Xs.assign(Xs, Xs + N);
+  c->Xf.assign(Xf, Xf + N + 1);
   c->D = dispatch_for(N);
   for (int w = 0; w < 4; w++) c->L[w] = default_launch(N, w);
   auto fail = [&](int code) {
@@ -245,6 +287,16 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   }
   c->nface2 = (int)f2.size();
   c->nface1 = (int)f1.size();
+  // face neighbours per cell (local face 1..4 -> cell across it, -1 at FREE faces)
+  std::vector<int4> nbr(NC, make_int4(-1, -1, -1, -1));
+  auto setn = [&](int cell, int lf, int other) {
+    int* v = reinterpret_cast<int*>(&nbr[cell]);
+    v[lf - 1] = other;
+  };
+  for (const int4& f : f2) {
+    setn(f.x, f.y, f.z);
+    setn(f.z, f.w, f.x);
+  }
 
   // ---- derived geometry
   const int NS = N * N, NF1 = (N + 1) * N, NFP = 2 * NF1, NG = 4 * (N + 1);
@@ -313,7 +365,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   for (int f = 0; f < c->nface1; f++)
     for (int nfp = 0; nfp < N; nfp++) fill(f1[f].x, f1[f].y, 1, nfp, fn1[(size_t)f * N + nfp]);
 
-  // ---- device arena
+  // ---- device arena (arena_plan_bytes below must follow the same sequence)
   const size_t nq = (size_t)NC * NS * 9, nfp = (size_t)NC * NFP;
   ArenaPlan P;
   size_t oQ = P.take<double>(nq), oQk0 = P.take<double>(nq), oQka = P.take<double>(nq);
@@ -326,8 +378,11 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
          oSe = P.take<double>(NC), omuf = P.take<double>((size_t)NC * 4), odiag = P.take<double>((size_t)NC * 2),
          of2 = P.take<int4>(f2.size() + 1), of1 = P.take<int2>(f1.size() + 1),
          ofn2 = P.take<FaceNorm>(fn2.size() + 1), ofn1 = P.take<FaceNorm>(fn1.size() + 1),
-         oeig = P.take<unsigned long long>(4), oerr = P.take<unsigned int>(4), ored = P.take<double>(8);
+         oeig = P.take<unsigned long long>(4), oerr = P.take<unsigned int>(4), ored = P.take<double>(8),
+         oact = P.take<int>(NC), onv = P.take<int>(NC), onbr = P.take<int4>(NC);
   c->arena_bytes = P.off;
+  if (P.off != arena_plan_bytes(N, NC, c->nface2, c->nface1, params->k_stage))
+    return fail(set_err(CHORUS_EINVAL, "internal: arena plan mismatch"));
   cudaError_t e = cudaMalloc(&c->arena, P.off);
   if (e != cudaSuccess)
     return fail(set_err(CHORUS_ENOMEM, "cudaMalloc(%zu bytes) failed: %s", P.off, cudaGetErrorString(e)));
@@ -367,6 +422,11 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   s.face1 = (const int2*)(A + of1);
   s.fn2 = (const FaceNorm*)(A + ofn2);
   s.fn1 = (const FaceNorm*)(A + ofn1);
+  s.act = (int*)(A + oact);
+  s.nv = (int*)(A + onv);
+  s.nbr = (const int4*)(A + onbr);
+  c->skip_option = 1;
+  s.skip = (params->mu == 0.0 && params->eta0 == 0.0) ? 1 : 0;
   s.eig = (unsigned long long*)(A + oeig);
   s.err = (unsigned int*)(A + oerr);
   c->red = (double*)(A + ored);
@@ -385,6 +445,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   up((void*)s.face1, f1.data(), f1.size() * sizeof(int2));
   up((void*)s.fn2, fn2.data(), fn2.size() * sizeof(FaceNorm));
   up((void*)s.fn1, fn1.data(), fn1.size() * sizeof(FaceNorm));
+  up((void*)s.nbr, nbr.data(), nbr.size() * sizeof(int4));
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return fail(set_err(CHORUS_ECUDA, "upload failed: %s", cudaGetErrorString(e)));
   int rc = ensure_ops(device, N, Lmat, Mmat, Xs, Xf);
@@ -422,8 +483,53 @@ int chorus_gpu_set_params(ChorusCtx* c, const ChorusParams* p) {
   c->sd.mu = p->mu;
   c->sd.eta0 = p->eta0;
   c->sd.artiv = p->ARTIV == 1;
+  c->sd.skip = (c->skip_option && p->mu == 0.0 && p->eta0 == 0.0) ? 1 : 0;
   drop_graphs(c);
   return CHORUS_OK;
+}
+
+int chorus_gpu_set_option(ChorusCtx* c, const char* name, int64_t value) {
+  if (!c || !name) return set_err(CHORUS_EINVAL, "null argument");
+  std::string n(name);
+  if (n == "diagnostics") {
+    c->diagnostics = value ? 1 : 0;
+  } else if (n == "skip_inactive_viscous") {
+    c->skip_option = value ? 1 : 0;
+    c->sd.skip = (c->skip_option && c->p.mu == 0.0 && c->p.eta0 == 0.0) ? 1 : 0;
+  } else if (n.rfind("epb_", 0) == 0 || n.rfind("threads_", 0) == 0) {
+    const char* pass[4] = {"e1", "e2", "e3", "ct"};
+    const bool epb = n[0] == 'e';
+    const std::string which = n.substr(epb ? 4 : 8);
+    int w = -1;
+    for (int i = 0; i < 4; i++)
+      if (which == pass[i]) w = i;
+    if (w < 0) return set_err(CHORUS_EINVAL, "unknown option %s", name);
+    if (epb) {
+      if (value < 1 || value > 64) return set_err(CHORUS_EINVAL, "%s=%lld outside 1..64", name, (long long)value);
+      c->L[w].epb = (int)value;
+    } else {
+      if (value < 32 || value > 256 || value % 32) return set_err(CHORUS_EINVAL, "%s=%lld must be 32..256, a multiple of 32", name, (long long)value);
+      c->L[w].threads = (int)value;
+    }
+  } else {
+    return set_err(CHORUS_EINVAL, "unknown option %s", name);
+  }
+  drop_graphs(c);
+  return CHORUS_OK;
+}
+
+int64_t chorus_gpu_get_option(ChorusCtx* c, const char* name) {
+  if (!c || !name) return -1;
+  std::string n(name);
+  if (n == "skip_inactive_viscous") return c->skip_option;
+  if (n == "diagnostics") return c->diagnostics;
+  if (n == "skip_active") return c->sd.skip;
+  const char* pass[4] = {"e1", "e2", "e3", "ct"};
+  for (int i = 0; i < 4; i++) {
+    if (n == std::string("epb_") + pass[i]) return c->L[i].epb;
+    if (n == std::string("threads_") + pass[i]) return c->L[i].threads;
+  }
+  return -1;
 }
 
 int chorus_gpu_upload_state(ChorusCtx* c, const double* Q) {
@@ -655,7 +761,7 @@ int iterations_gpu(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime, C
   };
   for (int s = 0; s < nsteps; s++) {
     *iter = *iter + 1;
-    const bool d = (*iter % 10) == 1;
+    const bool d = c->diagnostics && (*iter % 10) == 1;
     CK(cudaGraphLaunch(d ? c->g_diag : c->g_step, c->st));
     if (ctime) *ctime = *ctime + c->p.dt;
     if (d) {
@@ -777,6 +883,14 @@ int chorus_gpu_download_array(ChorusCtx* c, const char* name, double* out, int64
         std::memcpy(out + per * e, h.data() + ((size_t)e * NFP + (size_t)x.fam * NF1) * x.w, per * sizeof(double));
       return CHORUS_OK;
     }
+  if (n == "av_active" || n == "viscous_cells") {
+    if ((size_t)count != (size_t)NC) return set_err(CHORUS_EINVAL, "%s has %d elements", name, NC);
+    std::vector<int> hi(NC);
+    CK(cudaMemcpyAsync(hi.data(), n == "av_active" ? s.act : s.nv, NC * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (int e = 0; e < NC; e++) out[e] = hi[e];
+    return CHORUS_OK;
+  }
   if (n == "muAVfi" || n == "muAVfj") {
     if ((size_t)count != (size_t)NC * 18) return set_err(CHORUS_EINVAL, "%s has %d elements", name, NC * 18);
     int rc = pull(s.muf, (size_t)NC * 4, h);
@@ -937,6 +1051,13 @@ const double* chorus_mesh_darray(const ChorusMesh* mh, const char* name, int64_t
     }
   if (count) *count = 0;
   return nullptr;
+}
+
+int64_t chorus_mesh_device_bytes(const ChorusMesh* mh) {
+  if (!mh) return -1;
+  const Mesh& m = mh->m;
+  const int nface2 = (int)m.IBFINTER.size() + m.NPAIR, nface1 = (int)m.IBFREE.size();
+  return (int64_t)arena_plan_bytes(m.N, m.NCELL, nface2, nface1, m.params.k_stage);
 }
 
 int chorus_gpu_bind_mesh(const ChorusMesh* mh, int32_t device, ChorusCtx** ctx) {

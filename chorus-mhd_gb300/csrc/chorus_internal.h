@@ -80,6 +80,14 @@ struct SolveDev {
   const FaceNorm* fn2;          // [face][nfp]
   const int2* face1;            // (c, lf)
   const FaceNorm* fn1;          // [face][nfp] (ss unused)
+  // AV activity (used only when skip != 0, i.e. mu == 0 and eta0 == 0): act[e] = the
+  // cell's sensor is not below se_low; nv[e] = the cell or a face neighbour is active
+  // (the cell's viscous flux can be nonzero); nbr[e] = face neighbours (-1: none)
+  int skip;
+  int pad1;
+  int* act;
+  int* nv;
+  const int4* nbr;
   unsigned long long* eig;      // bit pattern of the stage's max wave speed (>= 0)
   unsigned int* err;            // error flags (bit 0: non-finite wave speed)
   double* diag;                 // per-cell diagnostic partial sums [e][2]

@@ -36,8 +36,14 @@ struct OpsN {
   double Xs[kMaxN];
 };
 
-// one copy per translation unit; upload_ops_tu() fills it
+// one copy per translation unit; upload_ops_n<N>() fills it
 static __constant__ OpsN c_ops;
+
+// operator accessors: the per-N kernels read their translation unit's single table,
+// the multi-solve kernels one table per N
+struct OpsTU {
+  __device__ static const OpsN& ops() { return c_ops; }
+};
 
 template <int N>
 struct D {
@@ -93,13 +99,10 @@ __device__ __forceinline__ void block_max_ull(unsigned long long v, unsigned lon
 // ---------------------------------------------------------------------------
 // E1: flux-point values, interior inviscid flux, AV sensor
 // ---------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor) {
+template <int N, class O>
+__device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int epb, int sensor, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
-  extern __shared__ double sm[];
-  const int e0 = blockIdx.x * epb;
-  const int cnt = min(epb, s.NC - e0);
-  if (cnt <= 0) return;
+
   double* sQ = sm;                    // [epb][NS][9]
   double* sT = sQ + epb * NS * 9;     // [epb][NS] sensor scratch
   double* sU = sT + epb * NS;         // [epb][NS]
@@ -121,7 +124,7 @@ __global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor) {
       for (int k = 0; k < 9; k++) {
         double a = 0.0;
 #pragma unroll
-        for (int sp = 0; sp < N; sp++) a += q[(jfp * N + sp) * 9 + k] * c_ops.L[ifp + (N + 1) * sp];
+        for (int sp = 0; sp < N; sp++) a += q[(jfp * N + sp) * 9 + k] * O::ops().L[ifp + (N + 1) * sp];
         qf[k] = a;
       }
     } else {
@@ -131,7 +134,7 @@ __global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor) {
       for (int k = 0; k < 9; k++) {
         double a = 0.0;
 #pragma unroll
-        for (int sp = 0; sp < N; sp++) a += q[(sp * N + ifp) * 9 + k] * c_ops.L[jfp + (N + 1) * sp];
+        for (int sp = 0; sp < N; sp++) a += q[(sp * N + ifp) * 9 + k] * O::ops().L[jfp + (N + 1) * sp];
         qf[k] = a;
       }
     }
@@ -149,14 +152,21 @@ __global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor) {
       for (int k = 0; k < 8; k++) fo[k] = F[k];
     }
   }
-  if (!sensor) return;
+  if (!sensor) {
+    if (s.skip)
+      for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+        s.act[e0 + e] = 0;
+        s.nv[e0 + e] = 0;
+      }
+    return;
+  }
   // AV sensor of variable 1 (AV.f90:15-82): Qsm = A rho A^T, Se = log10 sum((Qsm-rho)/rho)^2
   for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
     const int e = t / NS, p = t - e * NS, is = p % N, n = p / N;
     const double* q = sQ + e * NS * 9;
     double a = 0.0;
 #pragma unroll
-    for (int m = 0; m < N; m++) a += c_ops.A[is * N + m] * q[(n * N + m) * 9];
+    for (int m = 0; m < N; m++) a += O::ops().A[is * N + m] * q[(n * N + m) * 9];
     sT[e * NS + p] = a;  // T(is, n)
   }
   __syncthreads();
@@ -164,7 +174,7 @@ __global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor) {
     const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
     double a = 0.0;
 #pragma unroll
-    for (int n = 0; n < N; n++) a += c_ops.A[js * N + n] * sT[e * NS + n * N + is];
+    for (int n = 0; n < N; n++) a += O::ops().A[js * N + n] * sT[e * NS + n * N + is];
     const double rho = sQ[(e * NS + p) * 9];
     const double d = a - rho;
     sU[e * NS + p] = d * d / (rho * rho);
@@ -173,17 +183,58 @@ __global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor) {
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     double acc = 0.0;
     for (int p = 0; p < NS; p++) acc += sU[e * NS + p];
-    s.Se[e0 + e] = log10(acc);
+    const double se = log10(acc);
+    s.Se[e0 + e] = se;
+    if (s.skip) {
+      const int a = (se < -6.0) ? 0 : 1;  // NaN counts as active
+      s.act[e0 + e] = a;
+      s.nv[e0 + e] = a;
+    }
   }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor) {
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  e1_body<N, OpsTU>(s, e0, cnt, epb, sensor, sm);
+}
+
+// cells of this CTA whose gradients (mode 0) or viscous fluxes (mode 1) are needed,
+// compacted into a shared list; returns the count
+__device__ __forceinline__ int active_cells(const SolveDev& s, int e0, int cnt, int mode, int* list) {
+  __shared__ int n_act;
+  if (threadIdx.x == 0) {
+    int n = 0;
+    for (int e = 0; e < cnt; e++) {
+      const int c = e0 + e;
+      int need = 1;
+      if (s.skip) {
+        need = s.nv[c];
+        if (mode == 0 && !need) {
+          const int4 b = s.nbr[c];
+          need = (b.x >= 0 && s.nv[b.x]) || (b.y >= 0 && s.nv[b.y]) || (b.z >= 0 && s.nv[b.z]) ||
+                 (b.w >= 0 && s.nv[b.w]);
+        }
+      }
+      if (need) list[n++] = e;
+    }
+    n_act = n;
+  }
+  __syncthreads();
+  return n_act;
 }
 
 // ---------------------------------------------------------------------------
 // F1: Rusanov flux on every face point (interfaceflux / CYCLOCFLUX / BCFLUX)
 // ---------------------------------------------------------------------------
+// one face point t of the solve's two-sided (t < nface2*N) then FREE face points;
+// returns the bit pattern of its wave speed for the block max
 template <int N>
-__global__ void __launch_bounds__(256) k_f1(SolveDev s) {
+__device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t) {
   constexpr int NFP = D<N>::NFP;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int n2 = s.nface2 * N, n1 = s.nface1 * N;
   unsigned long long evb = 0ull;
   if (t < n2 + n1) {
@@ -222,6 +273,13 @@ __global__ void __launch_bounds__(256) k_f1(SolveDev s) {
 #pragma unroll
     for (int k = 0; k < 8; k++) fl[k] = fn.msl * Fh[k];
     s.Azf[gl] = az;
+    if (two && s.skip && nfp == 0) {
+      const int4 fc = s.face2[f];
+      if (s.act[fc.x] | s.act[fc.z]) {
+        s.nv[fc.x] = 1;
+        s.nv[fc.z] = 1;
+      }
+    }
     if (two) {
       double* fr = s.Fc + gr * 8;
 #pragma unroll
@@ -237,34 +295,61 @@ __global__ void __launch_bounds__(256) k_f1(SolveDev s) {
       }
     }
   }
+  return evb;
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_f1(SolveDev s) {
+  const unsigned long long evb = f1_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
   block_max_ull(evb, s.eig);
 }
 
 // ---------------------------------------------------------------------------
 // E2: gradients at solution points and their values at every flux point
 // ---------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb) {
+template <int N, class O>
+__device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int epb, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
-  extern __shared__ double sm[];
-  const int e0 = blockIdx.x * epb;
-  const int cnt = min(epb, s.NC - e0);
-  if (cnt <= 0) return;
+  __shared__ int list[64];
+
   double* sQ = sm;                  // [epb][NFP][9]
   double* sA = sQ + epb * NFP * 9;  // [epb][NFP]
   double* sG = sA + epb * NFP;      // [epb][NS][16]  (d*8 + k)
+  const int nact = active_cells(s, e0, cnt, 0, list);
   {
-    const double2* g = reinterpret_cast<const double2*>(s.Qvf + (size_t)e0 * NFP * 9);
-    double2* d = reinterpret_cast<double2*>(sQ);
-    const int n2 = cnt * NFP * 9 / 2;  // NFP even
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) d[i] = g[i];
     const double* ga = s.Azf + (size_t)e0 * NFP;
     for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) sA[i] = ga[i];
+    // flux-point states only for the cells whose gradients are needed
+    for (int i = threadIdx.x; i < nact * NFP * 9; i += blockDim.x) {
+      const int le = i / (NFP * 9), r = i - le * (NFP * 9), e = list[le];
+      sQ[e * NFP * 9 + r] = s.Qvf[((size_t)(e0 + e) * NFP) * 9 + r];
+    }
   }
   __syncthreads();
+  // grad A_z at every solution point of every cell (nablaAsp)
   for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
     const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
-    const double* w = s.gco + ((size_t)(e0 + e) * NS + p) * NG;
+    const size_t gs = (size_t)(e0 + e) * NS + p;
+    const double* w = s.gco + gs * NG;
+    const double* az = sA + e * NFP;
+    double ax = 0.0, ay = 0.0;
+#pragma unroll
+    for (int r = 0; r <= N; r++) {
+      const double a = az[js * (N + 1) + r];
+      const double b = az[NF1 + r * N + is];
+      ax += w[r] * a;
+      ax += w[(N + 1) + r] * b;
+      ay += w[2 * (N + 1) + r] * a;
+      ay += w[3 * (N + 1) + r] * b;
+    }
+    s.nAs[2 * gs] = ax;
+    s.nAs[2 * gs + 1] = ay;
+  }
+  // grad Q (variables 1-8) where needed (nablaQsp)
+  for (int t = threadIdx.x; t < nact * NS; t += blockDim.x) {
+    const int le = t / NS, p = t - le * NS, e = list[le], is = p % N, js = p / N;
+    const size_t gs = (size_t)(e0 + e) * NS + p;
+    const double* w = s.gco + gs * NG;
     double cx1[N + 1], cx2[N + 1], cy1[N + 1], cy2[N + 1];
 #pragma unroll
     for (int r = 0; r <= N; r++) {
@@ -274,7 +359,6 @@ __global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb) {
       cy2[r] = w[3 * (N + 1) + r];
     }
     const double* q = sQ + e * NFP * 9;
-    const size_t gs = (size_t)(e0 + e) * NS + p;
     double* out = s.nQs + gs * 18;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -293,23 +377,11 @@ __global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb) {
       sG[(e * NS + p) * 16 + k] = gx;
       sG[(e * NS + p) * 16 + 8 + k] = gy;
     }
-    const double* az = sA + e * NFP;
-    double ax = 0.0, ay = 0.0;
-#pragma unroll
-    for (int r = 0; r <= N; r++) {
-      const double a = az[js * (N + 1) + r];
-      const double b = az[NF1 + r * N + is];
-      ax += cx1[r] * a;
-      ax += cx2[r] * b;
-      ay += cy1[r] * a;
-      ay += cy2[r] * b;
-    }
-    s.nAs[2 * gs] = ax;
-    s.nAs[2 * gs + 1] = ay;
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < cnt * NFP; t += blockDim.x) {
-    const int e = t / NFP, fp = t - e * NFP;
+  // grad Q at every flux point where needed (nablaQ_interior_FP + face traces)
+  for (int t = threadIdx.x; t < nact * NFP; t += blockDim.x) {
+    const int le = t / NFP, fp = t - le * NFP, e = list[le];
     const double* G = sG + e * NS * 16;
     double acc[16];
 #pragma unroll
@@ -318,7 +390,7 @@ __global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb) {
       const int ifp = fp % (N + 1), jfp = fp / (N + 1);
 #pragma unroll
       for (int sp = 0; sp < N; sp++) {
-        const double l = c_ops.L[ifp + (N + 1) * sp];
+        const double l = O::ops().L[ifp + (N + 1) * sp];
 #pragma unroll
         for (int c = 0; c < 16; c++) acc[c] += G[(jfp * N + sp) * 16 + c] * l;
       }
@@ -326,7 +398,7 @@ __global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb) {
       const int r = fp - NF1, ifp = r % N, jfp = r / N;
 #pragma unroll
       for (int sp = 0; sp < N; sp++) {
-        const double l = c_ops.L[jfp + (N + 1) * sp];
+        const double l = O::ops().L[jfp + (N + 1) * sp];
 #pragma unroll
         for (int c = 0; c < 16; c++) acc[c] += G[(sp * N + ifp) * 16 + c] * l;
       }
@@ -340,16 +412,25 @@ __global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb) {
   }
 }
 
+template <int N>
+__global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb) {
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  e2_body<N, OpsTU>(s, e0, cnt, epb, sm);
+}
+
 // ---------------------------------------------------------------------------
 // F2: face-averaged gradients and face AV viscosity
 // ---------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(256) k_f2(SolveDev s, double eps_scale) {
+__device__ __forceinline__ void f2_point(const SolveDev& s, int t) {
   constexpr int NFP = D<N>::NFP;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int n2 = s.nface2 * N, n1 = s.nface1 * N;
+  if (t >= n2 + n1) return;
   const double eig = __longlong_as_double((long long)*s.eig);
-  const double eps0 = eig * s.hmsh / (double)(N - 1) * eps_scale;
+  const double eps0 = eig * s.hmsh / (double)(N - 1) * 1.0;
   if (t < n2) {
     const int f = t / N, nfp = t - f * N;
     const int4 fc = s.face2[f];
@@ -357,8 +438,9 @@ __global__ void __launch_bounds__(256) k_f2(SolveDev s, double eps_scale) {
     const size_t gr = (size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp);
     double* a = s.nQvf + gl * 18;
     double* b = s.nQvf + gr * 18;
+    const bool live = !s.skip || s.nv[fc.x] || s.nv[fc.z];
 #pragma unroll
-    for (int d = 0; d < 2; d++)
+    for (int d = 0; d < 2 * live; d++)
 #pragma unroll
       for (int k = 0; k < 8; k++) {
         const double v = 0.5 * a[9 * d + k] + 0.5 * b[9 * d + k];
@@ -380,38 +462,42 @@ __global__ void __launch_bounds__(256) k_f2(SolveDev s, double eps_scale) {
   }
 }
 
+template <int N>
+__global__ void __launch_bounds__(256) k_f2(SolveDev s) {
+  f2_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // E3: viscous + AV flux, divergence, A_z advection, RK update
 // ---------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(256) k_e3(SolveDev s, RKStage rk, int epb, int update) {
+template <int N, class O>
+__device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int epb, const RKStage& rk, int update, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
-  extern __shared__ double sm[];
-  const int e0 = blockIdx.x * epb;
-  const int cnt = min(epb, s.NC - e0);
-  if (cnt <= 0) return;
+
   double* sF = sm;                 // [epb][NFP][8] total flux Fv - F
   double* sD = sF + epb * NFP * 8; // [epb][NS] diagnostic partial sums
-  const bool visc = true;
-  for (int t = threadIdx.x; t < cnt * NFP; t += blockDim.x) {
-    const int e = t / NFP, fp = t - e * NFP, c = e0 + e;
+  __shared__ int list[64];
+  const int nact = active_cells(s, e0, cnt, 1, list);
+  {
+    const double* fi = s.Fc + (size_t)e0 * NFP * 8;
+    for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) sF[i] = -fi[i];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nact * NFP; t += blockDim.x) {
+    const int le = t / NFP, fp = t - le * NFP, e = list[le], c = e0 + e;
     const size_t g = (size_t)c * NFP + fp;
-    double F[8];
-    const double* fi = s.Fc + g * 8;
-#pragma unroll
-    for (int k = 0; k < 8; k++) F[k] = -fi[k];
     double mut = s.mu;
     if (s.artiv) {
       const double* mf = s.muf + 4 * c;
       if (fp < NF1) {
-        const double x = c_ops.Xf[fp % (N + 1)];
+        const double x = O::ops().Xf[fp % (N + 1)];
         mut += mf[3] * (1.0 - x) + mf[1] * x;
       } else {
-        const double x = c_ops.Xf[(fp - NF1) / N];
+        const double x = O::ops().Xf[(fp - NF1) / N];
         mut += mf[0] * (1.0 - x) + mf[2] * x;
       }
     }
-    if (visc && (mut != 0.0 || s.eta0 != 0.0)) {
+    if (mut != 0.0 || s.eta0 != 0.0) {
       double q[9], gq[18], Fv[8];
       const double* pq = s.Qvf + g * 9;
       const double* pg = s.nQvf + g * 18;
@@ -426,12 +512,10 @@ __global__ void __launch_bounds__(256) k_e3(SolveDev s, RKStage rk, int epb, int
       gq[8] = 0.0;
       gq[17] = 0.0;
       vflux_contra(q, gq, mut, s.eta0, s.gam, s.met[2 * g], s.met[2 * g + 1], Fv);
+      double* d = sF + (e * NFP + fp) * 8;
 #pragma unroll
-      for (int k = 1; k < 8; k++) F[k] += Fv[k];
+      for (int k = 1; k < 8; k++) d[k] += Fv[k];
     }
-    double* d = sF + (e * NFP + fp) * 8;
-#pragma unroll
-    for (int k = 0; k < 8; k++) d[k] = F[k];
   }
   __syncthreads();
   for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
@@ -443,8 +527,8 @@ __global__ void __launch_bounds__(256) k_e3(SolveDev s, RKStage rk, int epb, int
       double a = 0.0;
 #pragma unroll
       for (int r = 0; r <= N; r++) {
-        a += c_ops.M[r + (N + 1) * is] * Fe[(js * (N + 1) + r) * 8 + k];
-        a += c_ops.M[r + (N + 1) * js] * Fe[(NF1 + r * N + is) * 8 + k];
+        a += O::ops().M[r + (N + 1) * is] * Fe[(js * (N + 1) + r) * 8 + k];
+        a += O::ops().M[r + (N + 1) * js] * Fe[(NF1 + r * N + is) * 8 + k];
       }
       R[k] = a;
     }
@@ -511,19 +595,25 @@ __global__ void __launch_bounds__(256) k_e3(SolveDev s, RKStage rk, int epb, int
   }
 }
 
+template <int N>
+__global__ void __launch_bounds__(256) k_e3(SolveDev s, RKStage rk, int epb, int update) {
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  e3_body<N, OpsTU>(s, e0, cnt, epb, rk, update, sm);
+}
+
 // ---------------------------------------------------------------------------
 // CT projection (correct_B_via_curl_Az, setinitialcond.f90:82-91)
 //   mode 0: A_z at every flux point (into Qvf variable 9)
 //   mode 2: grad A_z from the face-averaged values, B <- B0 + curl A_z
 // (mode 1, the face average, is k_ctface)
 // ---------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(256) k_ct_elem(SolveDev s, int epb, int mode) {
+template <int N, class O>
+__device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt, int epb, int mode, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
-  extern __shared__ double sm[];
-  const int e0 = blockIdx.x * epb;
-  const int cnt = min(epb, s.NC - e0);
-  if (cnt <= 0) return;
+
   double* sA = sm;  // mode 0: [epb][NS] A_z at solution points; mode 2: [epb][NFP]
   if (mode == 0) {
     for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sA[i] = s.Q[((size_t)e0 * NS + i) * 9 + 8];
@@ -535,11 +625,11 @@ __global__ void __launch_bounds__(256) k_ct_elem(SolveDev s, int epb, int mode) 
       if (fp < NF1) {
         const int ifp = fp % (N + 1), jfp = fp / (N + 1);
 #pragma unroll
-        for (int sp = 0; sp < N; sp++) v += a[jfp * N + sp] * c_ops.L[ifp + (N + 1) * sp];
+        for (int sp = 0; sp < N; sp++) v += a[jfp * N + sp] * O::ops().L[ifp + (N + 1) * sp];
       } else {
         const int r = fp - NF1, ifp = r % N, jfp = r / N;
 #pragma unroll
-        for (int sp = 0; sp < N; sp++) v += a[sp * N + ifp] * c_ops.L[jfp + (N + 1) * sp];
+        for (int sp = 0; sp < N; sp++) v += a[sp * N + ifp] * O::ops().L[jfp + (N + 1) * sp];
       }
       s.Qvf[((size_t)(e0 + e) * NFP + fp) * 9 + 8] = v;
     }
@@ -569,9 +659,17 @@ __global__ void __launch_bounds__(256) k_ct_elem(SolveDev s, int epb, int mode) 
 }
 
 template <int N>
-__global__ void __launch_bounds__(256) k_ct_face(SolveDev s) {
+__global__ void __launch_bounds__(256) k_ct_elem(SolveDev s, int epb, int mode) {
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  ct_elem_body<N, OpsTU>(s, e0, cnt, epb, mode, sm);
+}
+
+template <int N>
+__device__ __forceinline__ void ctface_point(const SolveDev& s, int t) {
   constexpr int NFP = D<N>::NFP;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= s.nface2 * N) return;
   const int f = t / N, nfp = t - f * N;
   const int4 fc = s.face2[f];
@@ -580,6 +678,11 @@ __global__ void __launch_bounds__(256) k_ct_face(SolveDev s) {
   const double v = 0.5 * s.Qvf[gl * 9 + 8] + 0.5 * s.Qvf[gr * 9 + 8];
   s.Qvf[gl * 9 + 8] = v;
   s.Qvf[gr * 9 + 8] = v;
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_ct_face(SolveDev s) {
+  ctface_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // nablaQsp(v0..v1) (compflux.f90:107-157) from the current Qvf, 0-based variables

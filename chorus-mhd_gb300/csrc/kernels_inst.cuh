@@ -56,7 +56,7 @@ void launch_e2<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
 template <>
 void launch_f2<kN>(const SolveDev& s, cudaStream_t st) {
   const int n = (s.nface2 + s.nface1) * kN;
-  if (n > 0) k_f2<kN><<<(n + 255) / 256, 256, 0, st>>>(s, 1.0);
+  if (n > 0) k_f2<kN><<<(n + 255) / 256, 256, 0, st>>>(s);
 }
 template <>
 void launch_e3<kN>(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st) {

@@ -102,7 +102,9 @@ int chorus_gpu_download_state(ChorusCtx* ctx, double* Q);
  * "resid" (9,N,N,NC), "F1" (8,N+1,N,NC), "G2" (8,N,N+1,NC), "Qvfi"/"Qvfj" (9,..),
  * "Azfi"/"Azfj", "nablaQs" (9,2,N,N,NC), "nablaQvfi"/"nablaQvfj" (9,2,..),
  * "nablaAs" (2,N,N,NC), "muAVfi"/"muAVfj" (9,2,NC; only variable 1 is carried),
- * "SM_IND1" (NC; sensor of variable 1).  `count` must equal the array size. */
+ * "SM_IND1" (NC; sensor of variable 1), "av_active" / "viscous_cells" (NC; 0/1 flags of
+ * the last stage when skip_inactive_viscous is in effect).  `count` must equal the array
+ * size. */
 int chorus_gpu_download_array(ChorusCtx* ctx, const char* name, double* out, int64_t count);
 /* eigvmax of the last stage (AV.f90:145) and epsilon0 (AV.f90:148). */
 int chorus_gpu_get_eigvmax(ChorusCtx* ctx, double* eigvmax_g, double* epsilon0);
@@ -164,11 +166,76 @@ void* chorus_gpu_stream(ChorusCtx* ctx);
  * kernel with CUDA events around it; ms[0..4] = mean duration of E1, F1, E2, F2, E3
  * and ms[5] = mean duration of a whole stage. */
 int chorus_gpu_profile_stage(ChorusCtx* ctx, int32_t reps, double* ms);
+/* Runtime options of a context:
+ *   "diagnostics" (default 1): compute the norms of every tenth step in iterations_gpu;
+ *   "skip_inactive_viscous" (default 1): with mu = eta0 = 0 the viscous flux at a flux
+ *       point is exactly zero unless an adjacent face carries AV viscosity, and a cell's
+ *       gradients are needed only within two face rings of an AV-active cell; skip that
+ *       work (results are unchanged).  0 computes every cell (and fills every gradient
+ *       array for inspection).
+ *   "epb_e1" / "epb_e2" / "epb_e3" / "epb_ct" (1..64): cells per CTA of a cell pass;
+ *   "threads_e1" / ... (32..256, multiple of 32): threads per CTA.
+ * chorus_gpu_get_option returns the current value (-1 for an unknown name); the extra
+ * read-only name "skip_active" tells whether skipping is in effect. */
+int chorus_gpu_set_option(ChorusCtx* ctx, const char* name, int64_t value);
+int64_t chorus_gpu_get_option(ChorusCtx* ctx, const char* name);
 /* Kernel launches enqueued by one time step (5 stages + CT projection) and by the
  * extra diagnostic of every tenth step. */
 int chorus_gpu_launch_counts(ChorusCtx* ctx, int32_t* per_step, int32_t* per_diag);
 /* Device bytes held by ctx (state, work arrays, geometry). */
 int64_t chorus_gpu_device_bytes(ChorusCtx* ctx);
+
+/* ------------------------------------------------------------------------------
+ * Batched form: many independent solves (any N, size, problem, dt) advanced together,
+ * one persistent launch per pass over a per-cell work table.  A solve's results are
+ * the same alone and in a batch.  No reference counterpart (the reference runs one
+ * solve per MPI job).
+ * --------------------------------------------------------------------------- */
+int chorus_batch_create(int32_t device, ChorusBatch** batch);
+int chorus_batch_free(ChorusBatch* batch);
+/* Add a bound context (its state stays where it is; the caller keeps ownership and
+ * must not free it while it is in the batch).  *slot receives the solve's slot. */
+int chorus_batch_add(ChorusBatch* batch, ChorusCtx* ctx, int32_t* slot);
+int chorus_batch_remove(ChorusBatch* batch, int32_t slot);
+/* Enqueue nsteps time steps (5 RK stages + CT projection, no norms) of every solve in
+ * the batch, replayed from one CUDA graph; returns without waiting. */
+int chorus_batch_step(ChorusBatch* batch, int32_t nsteps);
+/* Wait for the batch and check the per-solve error flags (*err_slot = failing slot). */
+int chorus_batch_sync(ChorusBatch* batch, int32_t* err_slot);
+int chorus_batch_stream(ChorusBatch* batch, void** stream);
+int chorus_batch_info(ChorusBatch* batch, int32_t* n_solves, int32_t* cell_tiles, int32_t* face_tiles,
+                      int64_t* dofs);
+
+/* ------------------------------------------------------------------------------
+ * Serving form: a request loop with continuous batching (no reference counterpart).
+ * Requests arrive over time; at every step boundary the loop admits arrived requests
+ * in order while their device memory fits hbm_budget_bytes, sets each up (mesh maps,
+ * binding, initial state) while the previous step runs, packs all admitted solves into
+ * one batch step, and retires a solve after ceil(end_time/dt) steps.  mode 1 runs the
+ * plain sequential loop instead (one solve at a time, first come first served).
+ * --------------------------------------------------------------------------- */
+typedef struct ChorusServeRequest {
+  const char* case_dir; /* QUAD.INP + mesh files */
+  double arrival_s;     /* seconds after the start of the run (sorted ascending) */
+  double end_time;      /* physical end time of the solve */
+} ChorusServeRequest;
+typedef struct ChorusServeConfig {
+  int32_t device;
+  int32_t mode;              /* 0 continuous batching, 1 plain sequential */
+  int64_t hbm_budget_bytes;  /* 0 = no limit */
+  int32_t max_active;        /* 0 = no limit */
+  int32_t pad;
+} ChorusServeConfig;
+typedef struct ChorusServeResult {
+  double admit_s, finish_s, latency_s; /* seconds since start; latency = finish - arrival */
+  int64_t dof;
+  int32_t steps;
+  int32_t status; /* CHORUS_OK or the error of that request */
+} ChorusServeResult;
+int chorus_serve_run(const ChorusServeRequest* reqs, int32_t n, const ChorusServeConfig* cfg,
+                     ChorusServeResult* results, double* makespan_s);
+/* Device bytes chorus_gpu_bind_mesh would allocate for this mesh (admission control). */
+int64_t chorus_mesh_device_bytes(const ChorusMesh* mesh);
 
 /* ------------------------------------------------------------------------------
  * Host-side setup for callers without the Fortran setup chain: reads QUAD.INP and

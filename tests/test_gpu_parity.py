@@ -52,6 +52,7 @@ def test_one_stage_arrays_match_oracle(case_root, case):
     o.run(2)  # move away from the symmetric initial data
     Q = o.array("Q").copy()
     s = Solver(Mesh(d), initial_state=False)
+    s.set_option("skip_inactive_viscous", 0)  # fill every gradient array for comparison
     s.upload(Q)
     o.compresid()
     s.compresid()
@@ -123,3 +124,23 @@ def test_drop_in_sequence_matches_oracle(case_root):
         s.correct_B_via_curl_Az()
     assert_close(s.state(), o.array("Q"), RUN_TOL, "drop-in sequence")
     assert s.ctime == pytest.approx(o.getd("ctime"), rel=1e-15)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c.get("artiv", 1) and not c.get("mu")], ids=ids)
+def test_skipping_inactive_viscous_work_changes_nothing(case_root, case):
+    """With mu = eta0 = 0 the skipped work is an exact zero: the residual with skipping
+    equals the residual computed on every cell."""
+    d = make_case(case_root, **case)
+    o = oracle.Oracle(d)
+    o.run(2)
+    Q = o.array("Q").copy()
+    sz = reference_layout_sizes(case["N"], case["nx"] * case["ny"])
+    res = []
+    for opt in (0, 1):
+        s = Solver(Mesh(d), initial_state=False)
+        s.set_option("skip_inactive_viscous", opt)
+        assert s.get_option("skip_active") == opt
+        s.upload(Q)
+        s.compresid()
+        res.append(s.array("resid", sz["resid"]))
+    assert np.array_equal(res[0], res[1])
