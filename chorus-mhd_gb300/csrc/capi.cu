@@ -329,12 +329,13 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
           return fail(code);
         }
         invJ[(size_t)ic * NS + js * N + is] = 1.0 / J;
-        double* w = &gco[((size_t)ic * NS + js * N + is) * NG];
+        // [cell][weight][point]: a warp reading one weight of consecutive points is coalesced
+        double* w = &gco[(size_t)ic * NG * NS + js * N + is];
         for (int r = 0; r <= N; r++) {
-          w[r] = Mmat[r + (N + 1) * is] * S1at(0, 0, r, js, ic) / J;
-          w[(N + 1) + r] = Mmat[r + (N + 1) * js] * S2at(1, 0, is, r, ic) / J;
-          w[2 * (N + 1) + r] = Mmat[r + (N + 1) * is] * S1at(0, 1, r, js, ic) / J;
-          w[3 * (N + 1) + r] = Mmat[r + (N + 1) * js] * S2at(1, 1, is, r, ic) / J;
+          w[(size_t)r * NS] = Mmat[r + (N + 1) * is] * S1at(0, 0, r, js, ic) / J;
+          w[(size_t)((N + 1) + r) * NS] = Mmat[r + (N + 1) * js] * S2at(1, 0, is, r, ic) / J;
+          w[(size_t)(2 * (N + 1) + r) * NS] = Mmat[r + (N + 1) * is] * S1at(0, 1, r, js, ic) / J;
+          w[(size_t)(3 * (N + 1) + r) * NS] = Mmat[r + (N + 1) * js] * S2at(1, 1, is, r, ic) / J;
         }
       }
   }
@@ -867,6 +868,8 @@ int chorus_gpu_download_array(ChorusCtx* c, const char* name, double* out, int64
       if ((size_t)count != x.cnt) return set_err(CHORUS_EINVAL, "%s has %zu elements, not %lld", name, x.cnt, (long long)count);
       CK(cudaMemcpyAsync(out, x.p, x.cnt * sizeof(double), cudaMemcpyDeviceToHost, c->st));
       CK(cudaStreamSynchronize(c->st));
+      if (n == "SM_IND1")  // the device keeps the sensor sum; Se = log10(sum) (AV.f90:79)
+        for (size_t i = 0; i < x.cnt; i++) out[i] = std::log10(out[i]);
       return CHORUS_OK;
     }
   // per-cell flux-point blocks split into the family-1 / family-2 arrays

@@ -42,10 +42,10 @@ void initial_point(int problem, double gam, double x, double y, const double* B,
 //   nQvf       [e][fp][2][9]
 //   nAs        [e][js][is][2]
 //   met        [e][fp][2]    (S1(1,1),S1(1,2)) on family 1, (S2(2,1),S2(2,2)) on 2
-//   gco        [e][js][is][4][N+1] gradient weights Mmat*S/Jac (x-fam1, x-fam2,
+//   gco        [e][4(N+1)][js][is] gradient weights Mmat*S/Jac (x-fam1, x-fam2,
 //                            y-fam1, y-fam2)
 //   invJ       [e][js][is]
-//   Se         [e]           AV sensor of variable 1 (log10)
+//   Se         [e]           AV sensor sum of variable 1 (the reference's SM_IND(1) is log10 of it)
 //   muf        [e][4]        face-averaged AV viscosity per local face 1..4
 // ---------------------------------------------------------------------------
 struct FaceNorm {  // per two-sided face point: unit normal, magnorm*sign_l, sign_l*sign_r

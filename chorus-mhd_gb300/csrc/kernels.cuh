@@ -99,57 +99,94 @@ __device__ __forceinline__ void block_max_ull(unsigned long long v, unsigned lon
 // ---------------------------------------------------------------------------
 // E1: flux-point values, interior inviscid flux, AV sensor
 // ---------------------------------------------------------------------------
+// sum of v over the lanes of a warp (all lanes must call)
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// element-local flux-point index of the i-th interior flux point (i < 2N(N-1)):
+// family 1 with ifp = 1..N-1, then family 2 with jfp = 1..N-1
+template <int N>
+__device__ __forceinline__ int interior_fp(int i) {
+  constexpr int H = N * (N - 1);
+  if (i < H) {
+    const int jfp = i / (N - 1), ifp = 1 + i % (N - 1);
+    return jfp * (N + 1) + ifp;
+  }
+  const int r = i - H, jfp = 1 + r / N, ifp = r % N;
+  return D<N>::NF1 + jfp * N + ifp;
+}
+
 template <int N, class O>
 __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int epb, int sensor, double* sm) {
-  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
-
-  double* sQ = sm;                    // [epb][NS][9]
-  double* sT = sQ + epb * NS * 9;     // [epb][NS] sensor scratch
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NINT = 2 * N * (N - 1);
+  double* sQ = sm;                    // [epb][NS][9]   cell states
+  double* sT = sQ + epb * NS * 9;     // [epb][NS]      sensor scratch
   double* sU = sT + epb * NS;         // [epb][NS]
+  double* sV = sU + epb * NS;         // [epb][NFP][9]  flux-point values
+  double* sF = sV + epb * NFP * 9;    // [epb][NFP][8]  interior contravariant flux
+  double* sZ = sF + epb * NFP * 8;    // [epb][NFP]     interior A_z
+  double* sL = sZ + epb * NFP;        // Lmat (N+1, N)
+  double* sA = sL + (N + 1) * N;      // AV smoothing operator (N, N)
   {
+    // all global traffic of the pass is contiguous block copies (coalesced)
     const double* g = s.Q + (size_t)e0 * NS * 9;
     for (int i = threadIdx.x; i < cnt * NS * 9; i += blockDim.x) sQ[i] = g[i];
+    for (int i = threadIdx.x; i < (N + 1) * N; i += blockDim.x) sL[i] = O::ops().L[i];
+    for (int i = threadIdx.x; i < N * N; i += blockDim.x) sA[i] = O::ops().A[i];
   }
   __syncthreads();
-  const double gm1 = s.gam - 1.0;
-  for (int t = threadIdx.x; t < cnt * NFP; t += blockDim.x) {
-    const int e = t / NFP, fp = t - e * NFP;
-    const double* q = sQ + e * NS * 9;
-    double qf[9];
-    int lidx;
+  // interpolation to every flux point, one (cell, flux point, variable) per thread so
+  // that every lane of every warp does FP64 work
+  for (int t = threadIdx.x; t < cnt * NFP * 9; t += blockDim.x) {
+    const int k = t % 9, ef = t / 9, e = ef / NFP, fp = ef - e * NFP;
+    const double* q = sQ + e * NS * 9 + k;
+    double a = 0.0;
     if (fp < NF1) {
       const int ifp = fp % (N + 1), jfp = fp / (N + 1);
-      lidx = ifp;
 #pragma unroll
-      for (int k = 0; k < 9; k++) {
-        double a = 0.0;
-#pragma unroll
-        for (int sp = 0; sp < N; sp++) a += q[(jfp * N + sp) * 9 + k] * O::ops().L[ifp + (N + 1) * sp];
-        qf[k] = a;
-      }
+      for (int sp = 0; sp < N; sp++) a += q[(jfp * N + sp) * 9] * sL[ifp + (N + 1) * sp];
     } else {
       const int r = fp - NF1, ifp = r % N, jfp = r / N;
-      lidx = jfp;
 #pragma unroll
-      for (int k = 0; k < 9; k++) {
-        double a = 0.0;
-#pragma unroll
-        for (int sp = 0; sp < N; sp++) a += q[(sp * N + ifp) * 9 + k] * O::ops().L[jfp + (N + 1) * sp];
-        qf[k] = a;
-      }
+      for (int sp = 0; sp < N; sp++) a += q[(sp * N + ifp) * 9] * sL[jfp + (N + 1) * sp];
     }
+    sV[t] = a;
+  }
+  __syncthreads();
+  // contravariant inviscid flux at the interior flux points only
+  const double gm1 = s.gam - 1.0;
+  for (int t = threadIdx.x; t < cnt * NINT; t += blockDim.x) {
+    const int e = t / NINT, fp = interior_fp<N>(t - e * NINT);
+    const double* qf = sV + (e * NFP + fp) * 9;
     const size_t g = (size_t)(e0 + e) * NFP + fp;
-    double* dst = s.Qvf + g * 9;
+    const double sx = s.met[2 * g], sy = s.met[2 * g + 1];
+    double F[8];
+    iflux_contra(qf, sx, sy, gm1, F);
+    double* fo = sF + (e * NFP + fp) * 8;
 #pragma unroll
-    for (int k = 0; k < 9; k++) dst[k] = qf[k];
-    if (lidx > 0 && lidx < N) {
-      s.Azf[g] = qf[8];
-      const double sx = s.met[2 * g], sy = s.met[2 * g + 1];
-      double F[8];
-      iflux_contra(qf, sx, sy, gm1, F);
-      double* fo = s.Fc + g * 8;
-#pragma unroll
-      for (int k = 0; k < 8; k++) fo[k] = F[k];
+    for (int k = 0; k < 8; k++) fo[k] = F[k];
+    sZ[e * NFP + fp] = qf[8];
+  }
+  __syncthreads();
+  {
+    const size_t g0 = (size_t)e0 * NFP;
+    double* gv = s.Qvf + g0 * 9;
+    for (int i = threadIdx.x; i < cnt * NFP * 9; i += blockDim.x) gv[i] = sV[i];
+    // interior points only: face points of Fc / Azf belong to the face pass
+    double* gf = s.Fc + g0 * 8;
+    for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) {
+      const int fp = (i >> 3) % NFP;
+      const int lidx = fp < NF1 ? fp % (N + 1) : (fp - NF1) / N;
+      if (lidx > 0 && lidx < N) gf[i] = sF[i];
+    }
+    double* gz = s.Azf + g0;
+    for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
+      const int fp = i % NFP;
+      const int lidx = fp < NF1 ? fp % (N + 1) : (fp - NF1) / N;
+      if (lidx > 0 && lidx < N) gz[i] = sZ[i];
     }
   }
   if (!sensor) {
@@ -160,13 +197,15 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
       }
     return;
   }
-  // AV sensor of variable 1 (AV.f90:15-82): Qsm = A rho A^T, Se = log10 sum((Qsm-rho)/rho)^2
+  // AV sensor of variable 1 (AV.f90:15-82): Qsm = A rho A^T, sum ((Qsm-rho)/rho)^2.
+  // Se = log10(sum) is compared with -6 and -1 only; the sum itself is kept (Se < -6
+  // exactly when sum < 1e-6) and the logarithm is taken where the ramp needs it.
   for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
     const int e = t / NS, p = t - e * NS, is = p % N, n = p / N;
     const double* q = sQ + e * NS * 9;
     double a = 0.0;
 #pragma unroll
-    for (int m = 0; m < N; m++) a += O::ops().A[is * N + m] * q[(n * N + m) * 9];
+    for (int m = 0; m < N; m++) a += sA[is * N + m] * q[(n * N + m) * 9];
     sT[e * NS + p] = a;  // T(is, n)
   }
   __syncthreads();
@@ -174,21 +213,25 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
     const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
     double a = 0.0;
 #pragma unroll
-    for (int n = 0; n < N; n++) a += O::ops().A[js * N + n] * sT[e * NS + n * N + is];
+    for (int n = 0; n < N; n++) a += sA[js * N + n] * sT[e * NS + n * N + is];
     const double rho = sQ[(e * NS + p) * 9];
-    const double d = a - rho;
-    sU[e * NS + p] = d * d / (rho * rho);
+    const double d = (a - rho) * rcp_pos(rho);
+    sU[e * NS + p] = d * d;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+  // one warp per cell sums its points
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (int e = warp; e < cnt; e += nwarp) {
     double acc = 0.0;
-    for (int p = 0; p < NS; p++) acc += sU[e * NS + p];
-    const double se = log10(acc);
-    s.Se[e0 + e] = se;
-    if (s.skip) {
-      const int a = (se < -6.0) ? 0 : 1;  // NaN counts as active
-      s.act[e0 + e] = a;
-      s.nv[e0 + e] = a;
+    for (int p = lane; p < NS; p += 32) acc += sU[e * NS + p];
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      s.Se[e0 + e] = acc;
+      if (s.skip) {
+        const int a = (acc < 1e-6) ? 0 : 1;  // NaN counts as active
+        s.act[e0 + e] = a;
+        s.nv[e0 + e] = a;
+      }
     }
   }
 }
@@ -315,8 +358,10 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
   double* sQ = sm;                  // [epb][NFP][9]
   double* sA = sQ + epb * NFP * 9;  // [epb][NFP]
   double* sG = sA + epb * NFP;      // [epb][NS][16]  (d*8 + k)
+  double* sL = sG + epb * NS * 16;  // Lmat (N+1, N)
   const int nact = active_cells(s, e0, cnt, 0, list);
   {
+    for (int i = threadIdx.x; i < (N + 1) * N; i += blockDim.x) sL[i] = O::ops().L[i];
     const double* ga = s.Azf + (size_t)e0 * NFP;
     for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) sA[i] = ga[i];
     // flux-point states only for the cells whose gradients are needed
@@ -330,17 +375,17 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
   for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
     const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
     const size_t gs = (size_t)(e0 + e) * NS + p;
-    const double* w = s.gco + gs * NG;
+    const double* w = s.gco + (size_t)(e0 + e) * NG * NS + p;
     const double* az = sA + e * NFP;
     double ax = 0.0, ay = 0.0;
 #pragma unroll
     for (int r = 0; r <= N; r++) {
       const double a = az[js * (N + 1) + r];
       const double b = az[NF1 + r * N + is];
-      ax += w[r] * a;
-      ax += w[(N + 1) + r] * b;
-      ay += w[2 * (N + 1) + r] * a;
-      ay += w[3 * (N + 1) + r] * b;
+      ax += w[r * NS] * a;
+      ax += w[((N + 1) + r) * NS] * b;
+      ay += w[(2 * (N + 1) + r) * NS] * a;
+      ay += w[(3 * (N + 1) + r) * NS] * b;
     }
     s.nAs[2 * gs] = ax;
     s.nAs[2 * gs + 1] = ay;
@@ -349,14 +394,14 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
   for (int t = threadIdx.x; t < nact * NS; t += blockDim.x) {
     const int le = t / NS, p = t - le * NS, e = list[le], is = p % N, js = p / N;
     const size_t gs = (size_t)(e0 + e) * NS + p;
-    const double* w = s.gco + gs * NG;
+    const double* w = s.gco + (size_t)(e0 + e) * NG * NS + p;
     double cx1[N + 1], cx2[N + 1], cy1[N + 1], cy2[N + 1];
 #pragma unroll
     for (int r = 0; r <= N; r++) {
-      cx1[r] = w[r];
-      cx2[r] = w[(N + 1) + r];
-      cy1[r] = w[2 * (N + 1) + r];
-      cy2[r] = w[3 * (N + 1) + r];
+      cx1[r] = w[r * NS];
+      cx2[r] = w[((N + 1) + r) * NS];
+      cy1[r] = w[(2 * (N + 1) + r) * NS];
+      cy2[r] = w[(3 * (N + 1) + r) * NS];
     }
     const double* q = sQ + e * NFP * 9;
     double* out = s.nQs + gs * 18;
@@ -390,7 +435,7 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
       const int ifp = fp % (N + 1), jfp = fp / (N + 1);
 #pragma unroll
       for (int sp = 0; sp < N; sp++) {
-        const double l = O::ops().L[ifp + (N + 1) * sp];
+        const double l = sL[ifp + (N + 1) * sp];
 #pragma unroll
         for (int c = 0; c < 16; c++) acc[c] += G[(jfp * N + sp) * 16 + c] * l;
       }
@@ -398,7 +443,7 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
       const int r = fp - NF1, ifp = r % N, jfp = r / N;
 #pragma unroll
       for (int sp = 0; sp < N; sp++) {
-        const double l = O::ops().L[jfp + (N + 1) * sp];
+        const double l = sL[jfp + (N + 1) * sp];
 #pragma unroll
         for (int c = 0; c < 16; c++) acc[c] += G[(sp * N + ifp) * 16 + c] * l;
       }
@@ -474,13 +519,20 @@ template <int N, class O>
 __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int epb, const RKStage& rk, int update, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
 
-  double* sF = sm;                 // [epb][NFP][8] total flux Fv - F
-  double* sD = sF + epb * NFP * 8; // [epb][NS] diagnostic partial sums
+  double* sF = sm;                  // [epb][NFP][8] total flux Fv - F
+  double* sD = sF + epb * NFP * 8;  // [epb][NS] diagnostic partial sums
+  double* sQ = sD + epb * NS;       // [epb][NS][9] state of the block's cells
+  double* sR = sQ + epb * NS * 9;   // [epb][NS][9] residual
+  double* sM = sR + epb * NS * 9;   // Mmat (N+1, N)
   __shared__ int list[64];
   const int nact = active_cells(s, e0, cnt, 1, list);
   {
+    // every global access of the pass is a contiguous block copy (coalesced)
     const double* fi = s.Fc + (size_t)e0 * NFP * 8;
     for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) sF[i] = -fi[i];
+    const double* gq = s.Q + (size_t)e0 * NS * 9;
+    for (int i = threadIdx.x; i < cnt * NS * 9; i += blockDim.x) sQ[i] = gq[i];
+    for (int i = threadIdx.x; i < (N + 1) * N; i += blockDim.x) sM[i] = O::ops().M[i];
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nact * NFP; t += blockDim.x) {
@@ -518,79 +570,63 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
     }
   }
   __syncthreads();
+  // divergence of the total flux, one (cell, point, variable) per thread
+  for (int t = threadIdx.x; t < cnt * NS * 8; t += blockDim.x) {
+    const int k = t % 8, ep = t / 8, e = ep / NS, p = ep - e * NS, is = p % N, js = p / N;
+    const double* Fe = sF + e * NFP * 8 + k;
+    double a = 0.0;
+#pragma unroll
+    for (int r = 0; r <= N; r++) {
+      a += sM[r + (N + 1) * is] * Fe[(js * (N + 1) + r) * 8];
+      a += sM[r + (N + 1) * js] * Fe[(NF1 + r * N + is) * 8];
+    }
+    sR[ep * 9 + k] = a * s.invJ[(size_t)(e0 + e) * NS + p];
+  }
+  // A_z advection (resid(9), compresid.f90:45-47) at every solution point
   for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
-    const int e = t / NS, p = t - e * NS, is = p % N, js = p / N, c = e0 + e;
-    const double* Fe = sF + e * NFP * 8;
-    double R[9];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-      double a = 0.0;
-#pragma unroll
-      for (int r = 0; r <= N; r++) {
-        a += O::ops().M[r + (N + 1) * is] * Fe[(js * (N + 1) + r) * 8 + k];
-        a += O::ops().M[r + (N + 1) * js] * Fe[(NF1 + r * N + is) * 8 + k];
-      }
-      R[k] = a;
-    }
-    const size_t gs = (size_t)c * NS + p;
-    const double ij = s.invJ[gs];
-#pragma unroll
-    for (int k = 0; k < 8; k++) R[k] *= ij;
-    double* Qp = s.Q + gs * 9;
-    double q[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) q[k] = Qp[k];
-    const double ri = 1.0 / q[0];
+    const int e = t / NS, p = t - e * NS;
+    const size_t gs = (size_t)(e0 + e) * NS + p;
+    const double* q = sQ + t * 9;
+    const double ri = rcp_pos(q[0]);
     const double ax = s.nAs[2 * gs] - s.B0y, ay = s.nAs[2 * gs + 1] + s.B0x;
-    R[8] = -(q[1] * ri * ax + q[2] * ri * ay);
-    if (rk.write_resid) {
-      double* ro = s.resid + gs * 9;
-#pragma unroll
-      for (int k = 0; k < 9; k++) ro[k] = R[k];
-    }
-    if (rk.diag) {
-      double acc = 0.0;
-#pragma unroll
-      for (int k = 0; k < 9; k++) acc += R[k] * R[k];
-      sD[e * NS + p] = acc;
-    }
-    if (update) {
-      if (rk.save_old) {
-#pragma unroll
-        for (int k = 0; k < 9; k++) rk.save_old[gs * 9 + k] = q[k];
-      }
-      if (rk.save_R) {
-#pragma unroll
-        for (int k = 0; k < 9; k++) rk.save_R[gs * 9 + k] = R[k];
-      }
-      double qn[9];
-#pragma unroll
-      for (int k = 0; k < 9; k++) qn[k] = rk.cQ * q[k] + rk.cR * R[k];
-      for (int j = 0; j < rk.nsrc; j++) {
-        const double* sp = rk.src[j] + gs * 9;
-        const double cj = rk.c[j];
-#pragma unroll
-        for (int k = 0; k < 9; k++) qn[k] += cj * sp[k];
-      }
-      if (rk.R0) {
-        const double* r0 = rk.R0 + gs * 9;
-#pragma unroll
-        for (int k = 0; k < 9; k++) qn[k] += rk.cR0 * r0[k];
-      }
-#pragma unroll
-      for (int k = 0; k < 9; k++) Qp[k] = qn[k];
-      if (rk.save_new) {
-#pragma unroll
-        for (int k = 0; k < 9; k++) rk.save_new[gs * 9 + k] = qn[k];
-      }
-    }
+    sR[t * 9 + 8] = -(q[1] * ri * ax + q[2] * ri * ay);
   }
   if (rk.diag) {
     __syncthreads();
-    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
+      const double* r = sR + t * 9;
       double acc = 0.0;
-      for (int p = 0; p < NS; p++) acc += sD[e * NS + p];
-      s.diag[2 * (e0 + e)] = acc;
+#pragma unroll
+      for (int k = 0; k < 9; k++) acc += r[k] * r[k];
+      sD[t] = acc;
+    }
+  }
+  __syncthreads();
+  // stage update, elementwise over the block's contiguous state (RK_S5P3 / FiveStageRk)
+  {
+    const size_t g0 = (size_t)e0 * NS * 9;
+    const int n = cnt * NS * 9;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double q = sQ[i], r = sR[i];
+      const size_t g = g0 + i;
+      if (rk.write_resid) s.resid[g] = r;
+      if (!update) continue;
+      double qn = rk.cQ * q + rk.cR * r;
+      for (int j = 0; j < rk.nsrc; j++) qn += rk.c[j] * rk.src[j][g];
+      if (rk.R0) qn += rk.cR0 * rk.R0[g];
+      s.Q[g] = qn;
+      if (rk.save_old) rk.save_old[g] = q;
+      if (rk.save_new) rk.save_new[g] = qn;
+      if (rk.save_R) rk.save_R[g] = r;
+    }
+  }
+  if (rk.diag) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int e = warp; e < cnt; e += nwarp) {
+      double acc = 0.0;
+      for (int p = lane; p < NS; p += 32) acc += sD[e * NS + p];
+      acc = warp_sum(acc);
+      if (lane == 0) s.diag[2 * (e0 + e)] = acc;
     }
   }
 }
@@ -639,16 +675,16 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
     for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
       const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
       const size_t gs = (size_t)(e0 + e) * NS + p;
-      const double* w = s.gco + gs * NG;
+      const double* w = s.gco + (size_t)(e0 + e) * NG * NS + p;
       const double* a = sA + e * NFP;
       double gx = 0.0, gy = 0.0;
 #pragma unroll
       for (int r = 0; r <= N; r++) {
         const double fa = a[js * (N + 1) + r], fb = a[NF1 + r * N + is];
-        gx += w[r] * fa;
-        gx += w[(N + 1) + r] * fb;
-        gy += w[2 * (N + 1) + r] * fa;
-        gy += w[3 * (N + 1) + r] * fb;
+        gx += w[r * NS] * fa;
+        gx += w[((N + 1) + r) * NS] * fb;
+        gy += w[(2 * (N + 1) + r) * NS] * fa;
+        gy += w[(3 * (N + 1) + r) * NS] * fb;
       }
       s.nQs[gs * 18 + 8] = gx;
       s.nQs[gs * 18 + 9 + 8] = gy;
@@ -692,17 +728,17 @@ __global__ void __launch_bounds__(256) k_nqsp(SolveDev s, int v0, int v1) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= s.NC * NS) return;
   const int c = t / NS, p = t - c * NS, is = p % N, js = p / N;
-  const double* w = s.gco + (size_t)t * NG;
+  const double* w = s.gco + (size_t)c * NG * NS + p;
   const double* q = s.Qvf + (size_t)c * NFP * 9;
   for (int k = v0; k <= v1; k++) {
     double gx = 0.0, gy = 0.0;
 #pragma unroll
     for (int r = 0; r <= N; r++) {
       const double fa = q[(js * (N + 1) + r) * 9 + k], fb = q[(NF1 + r * N + is) * 9 + k];
-      gx += w[r] * fa;
-      gx += w[(N + 1) + r] * fb;
-      gy += w[2 * (N + 1) + r] * fa;
-      gy += w[3 * (N + 1) + r] * fb;
+      gx += w[r * NS] * fa;
+      gx += w[((N + 1) + r) * NS] * fb;
+      gy += w[(2 * (N + 1) + r) * NS] * fa;
+      gy += w[(3 * (N + 1) + r) * NS] * fb;
     }
     s.nQs[(size_t)t * 18 + k] = gx;
     s.nQs[(size_t)t * 18 + 9 + k] = gy;

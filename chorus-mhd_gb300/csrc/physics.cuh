@@ -11,12 +11,30 @@ namespace chorus {
 constexpr double kLambda = -2.0 / 3.0;  // setup2d.f90:70
 constexpr double kPrandt = 0.72;        // setup2d.f90:71
 
+// 1/x for the positive, normal densities of the path: the hardware approximation
+// (PTX rcp.approx.ftz.f64, about 20 correct bits) refined by two Newton-Raphson steps
+// r <- r + r(1 - x r), each doubling the correct bits; within one ulp of 1/x, and 4
+// FP64 FMAs instead of the longer IEEE-rounded division sequence.
+__host__ __device__ __forceinline__ double rcp_pos(double x) {
+#ifdef __CUDA_ARCH__
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  return r;
+#else
+  return 1.0 / x;
+#endif
+}
+
 // Contravariant ideal-MHD flux F*sx + G*sy of getIfluxvectors (getrusanov.f90:111-153)
 // as used by inviscid_flux_interior (compflux.f90:77-78, 96-97).
 __host__ __device__ __forceinline__ void iflux_contra(const double* q, double sx, double sy, double gm1,
                                                       double* F) {
   const double rho = q[0], ru = q[1], rv = q[2], rw = q[3], E = q[4], Bx = q[5], By = q[6], Bz = q[7];
-  const double ri = 1.0 / rho;
+  const double ri = rcp_pos(rho);
   const double u = ru * ri, v = rv * ri, w = rw * ri;
   const double B2 = Bx * Bx + By * By + Bz * Bz;
   const double ke = ru * u + rv * v + rw * w;
@@ -49,7 +67,7 @@ __host__ __device__ __forceinline__ void rusanov_core(const double* ql, const do
   for (int side = 0; side < 2; side++) {
     const double* q = qs[side];
     double* F = Fs[side];
-    const double ri = 1.0 / q[0];
+    const double ri = rcp_pos(q[0]);
     const double u = ri * q[1], v = ri * q[2], w = ri * q[3];
     const double Bx = q[5], By = q[6], Bz = q[7];
     const double B2 = Bx * Bx + By * By + Bz * Bz;
@@ -69,7 +87,7 @@ __host__ __device__ __forceinline__ void rusanov_core(const double* ql, const do
     vn[side] = Vn;
   }
   const double Bx = 0.5 * (ql[5] + qr[5]), By = 0.5 * (ql[6] + qr[6]), Bz = 0.5 * (ql[7] + qr[7]);
-  const double irs = 1.0 / (ql[0] + qr[0]);
+  const double irs = rcp_pos(ql[0] + qr[0]);
   const double ca = gam * (pgl + pgr) * irs;
   const double cd = (Bx * Bx + By * By + Bz * Bz) * (2.0 * irs);
   const double bn = Bx * ux + By * uy;
@@ -92,7 +110,7 @@ __host__ __device__ __forceinline__ void rusanov_core(const double* ql, const do
 __host__ __device__ __forceinline__ void vflux_contra(const double* q, const double* g, double mut, double eta0,
                                                       double gam, double sx, double sy, double* Fc) {
   const double rho = q[0], Bx = q[5], By = q[6], Bz = q[7];
-  const double ri = 1.0 / rho;
+  const double ri = rcp_pos(rho);
   const double u = q[1] * ri, v = q[2] * ri, w = q[3] * ri;
   const double NU = u * u + v * v + w * w;
   const double B2 = Bx * Bx + By * By + Bz * Bz;
@@ -135,10 +153,13 @@ __host__ __device__ __forceinline__ void vflux_contra(const double* q, const dou
   Fc[7] = f7 * sx + g7 * sy;
 }
 
-// muAV of variable 1 from the sensor (AV.f90:157-172 with se_low=-6, se_high=-1).
-__host__ __device__ __forceinline__ double av_mu(double se, double eps0) {
-  if (se < -6.0) return 0.0;
-  if (se > -1.0) return eps0;
+// muAV of variable 1 (AV.f90:157-172 with se_low=-6, se_high=-1) from the sensor sum
+// ssum = sum ((Qsm-rho)/rho)^2 of a cell, Se = log10(ssum): zero below 1e-6, epsilon0
+// above 0.1 (the ramp is continuous at both ends), the sine ramp in between.
+__host__ __device__ __forceinline__ double av_mu(double ssum, double eps0) {
+  if (ssum < 1e-6) return 0.0;
+  if (ssum > 0.1) return eps0;
+  const double se = log10(ssum);
   const double s0 = -3.5, kr = 2.5, pi = 3.14159265358979323846;
   return eps0 / 2.0 * (1.0 + sin(pi * (se - s0) / 2.0 / kr));
 }
