@@ -129,37 +129,18 @@ class ClockSampler:
 
 
 def dist_setup(args):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-        backend = "nccl"
-        try:
-            import torch
-            if not torch.cuda.is_available():
-                backend = "gloo"
-        except Exception:
-            backend = "gloo"
-        dist.init_process_group(backend=backend)
-    return world, rank, local
+    from chorus_mhd import dist
+    return dist.init()
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    from chorus_mhd import dist
+    dist.barrier(world)
 
 
 def max_over_ranks(world, x: float) -> float:
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
-    t = torch.tensor([x], dtype=torch.float64, device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from chorus_mhd import dist
+    return dist.max_over_ranks(world, x)
 
 
 def run_gpu(args):
@@ -224,10 +205,9 @@ def run_gpu(args):
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        sol.upload(qh)
+        sol.upload(qh)          # H2D from pinned host memory
         sol.iterations(1)
-        out = sol.state()
-        qh[:] = out
+        sol.state(out=qh)       # D2H into the same pinned buffer
     t1 = time.perf_counter()
     e2e_s = max_over_ranks(world, t1 - t0)
     e2e = {"value": world * dof * 5 * e2e_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 8 * sol.nq,
@@ -281,7 +261,10 @@ def run_ensemble(args, device, tmp):
     import numpy as np
     import torch
     from chorus_mhd import Batch, Mesh, Solver, ensemble
-    specs = ensemble.draw(count=args.ensemble_count)
+    from chorus_mhd import dist
+    world, rank, _ = dist.env()
+    # whole solves shard across ranks (no data-path exchange)
+    specs = dist.shard(ensemble.draw(count=args.ensemble_count), world, rank)
     t0 = time.perf_counter()
     dirs = ensemble.write_all(specs, os.path.join(tmp, "ensemble"))
     solvers = []
@@ -290,17 +273,19 @@ def run_ensemble(args, device, tmp):
         s.set_option("diagnostics", 0)
         solvers.append(s)
     t_setup = time.perf_counter() - t0
-    dof = sum(s.ncell * s.N * s.N for s in solvers)
+    dof_local = sum(s.ncell * s.N * s.N for s in solvers)
+    dof = int(dist.sum_over_ranks(world, float(dof_local)))
     K = args.ensemble_steps
     # plain loop: warm-up builds every solve's graph
     for s in solvers:
         s.iterations(1)
     torch.cuda.synchronize()
+    dist.barrier(world)
     t0 = time.perf_counter()
     for s in solvers:
         s.iterations(K)
     torch.cuda.synchronize()
-    t_plain = time.perf_counter() - t0
+    t_plain = dist.max_over_ranks(world, time.perf_counter() - t0)
     b = Batch(device)
     for s in solvers:
         b.add(s)
@@ -309,13 +294,14 @@ def run_ensemble(args, device, tmp):
     stream = torch.cuda.ExternalStream(b.stream_handle(), device=device)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    dist.barrier(world)
     t0 = time.perf_counter()
     e0.record(stream)
     b.step(K)
     e1.record(stream)
     b.sync()
-    t_batch = time.perf_counter() - t0
-    ms_batch = e0.elapsed_time(e1)
+    t_batch = dist.max_over_ranks(world, time.perf_counter() - t0)
+    ms_batch = dist.max_over_ranks(world, e0.elapsed_time(e1))
     info = b.info()
     finite = all(bool(np.isfinite(s.state()).all()) for s in solvers[:8])
     b.close()
@@ -324,7 +310,8 @@ def run_ensemble(args, device, tmp):
     Ns = {}
     for s in solvers:
         Ns[s.N] = Ns.get(s.N, 0) + 1
-    return {"solves": len(solvers), "dof": dof, "cells": sum(s.ncell for s in solvers), "steps": K,
+    return {"solves": int(dist.sum_over_ranks(world, float(len(solvers)))), "dof": dof,
+            "cells": int(dist.sum_over_ranks(world, float(sum(s.ncell for s in solvers)))), "steps": K,
             "N_counts": {str(k): v for k, v in sorted(Ns.items())}, "setup_s": t_setup,
             "batched": {"value": dof * 5 * K / (ms_batch / 1e3), "unit": METRIC, "ms_per_step": ms_batch / K,
                         "wall_ms_per_step": t_batch * 1e3 / K, "cell_tiles": info["cell_tiles"],

@@ -50,6 +50,7 @@ class ChorusDiag(ctypes.Structure):
 SIGNATURES = {
     "chorus_gpu_last_error": (c_char_p, []),
     "chorus_gpu_version": (c_char_p, []),
+    "chorus_gpu_device_name": (c_int, [c_int, c_char_p, c_int]),
     "chorus_gpu_bind": (c_int, [P(ChorusDims), ip, ip, ip, ip, ip, ip, dp, dp, dp, dp, dp, dp, dp,
                                 P(ChorusParams), c_int, P(c_void_p)]),
     "chorus_gpu_free": (c_int, [c_void_p]),

@@ -35,8 +35,8 @@ def cache_path(gpu_name: str) -> str:
 
 def _smem_bytes(N: int, pass_: str, epb: int) -> int:
     NS, NFP = N * N, 2 * (N + 1) * N
-    per = {"e1": NS * 9 + 2 * NS + NFP * 18, "e2": NFP * 9 + NFP + NS * 16,
-           "e3": NFP * 8 + NS + 2 * NS * 9, "ct": NFP}[pass_]
+    per = {"e1": NS * 9 + 2 * NS + NFP * 18, "e2": NFP * 9 + NS * 16,
+           "e3": NFP * 10 + NS * 22, "ct": NFP}[pass_]
     return 8 * (epb * per + 2 * (N + 1) * N)
 
 
@@ -77,8 +77,8 @@ def tune_order(N: int, device: int = 0, cells_per_side: int | None = None, reps:
 
 
 def tune(orders=(3, 4, 5, 6), device: int = 0) -> dict:
-    import torch
-    name = torch.cuda.get_device_name(device)
+    from .solver import device_name
+    name = device_name(device)
     out = {"gpu": name, "orders": {}}
     for N in orders:
         out["orders"][str(N)] = tune_order(N, device)
@@ -89,12 +89,30 @@ def tune(orders=(3, 4, 5, 6), device: int = 0) -> dict:
     return out
 
 
+SHIPPED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned")
+
+
+def shipped_path(gpu_name: str) -> str:
+    safe = "".join(c if c.isalnum() else "_" for c in gpu_name)
+    return os.path.join(SHIPPED, "tune_%s.json" % safe)
+
+
+_TABLES: dict = {}
+
+
 def load(gpu_name: str) -> dict | None:
-    p = cache_path(gpu_name)
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f)
-    return None
+    """The user's cache for this GPU model if present, else the table shipped with the
+    package (tuned on this model and committed)."""
+    if gpu_name in _TABLES:
+        return _TABLES[gpu_name]
+    table = None
+    for p in (cache_path(gpu_name), shipped_path(gpu_name)):
+        if os.path.exists(p):
+            with open(p) as f:
+                table = json.load(f)
+            break
+    _TABLES[gpu_name] = table
+    return table
 
 
 def apply(solver, table: dict | None) -> bool:

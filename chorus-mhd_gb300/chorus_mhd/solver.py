@@ -75,16 +75,29 @@ class Mesh:
             pass
 
 
-class Solver:
-    """One solve resident on one GPU; method names follow the reference routines."""
+def device_name(device: int = 0) -> str:
+    buf = ctypes.create_string_buffer(256)
+    check(_lib.load().chorus_gpu_device_name(int(device), buf, 256))
+    return buf.value.decode()
 
-    def __init__(self, mesh: Mesh, device: int = 0, initial_state: bool = True):
+
+class Solver:
+    """One solve resident on one GPU; method names follow the reference routines.
+
+    tuned=True applies the autotuned launch shapes of this GPU model, if a table exists
+    (chorus_mhd.autotune)."""
+
+    def __init__(self, mesh: Mesh, device: int = 0, initial_state: bool = True, tuned: bool = True):
         self.L = _lib.load()
         self.mesh = mesh
         ctx = ctypes.c_void_p()
         check(self.L.chorus_gpu_bind_mesh(mesh._h, device, ctypes.byref(ctx)))
         self._ctx = ctx
         self.N, self.ncell = mesh.N, mesh.ncell
+        self.tuned = False
+        if tuned:
+            from . import autotune
+            self.tuned = autotune.apply(self, autotune.load(device_name(device)))
         self.nq = 9 * self.N * self.N * self.ncell
         self.iter = 0
         self.ctime = 0.0
@@ -104,8 +117,11 @@ class Solver:
         assert Q.size == self.nq
         check(self.L.chorus_gpu_upload_state(self._ctx, _dp(Q)))
 
-    def state(self) -> np.ndarray:
-        Q = np.empty(self.nq)
+    def state(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Download Q (the reference's Q(9,N,N,NCELL), flat); into `out` if given
+        (e.g. a pinned buffer, so the copy runs at full link speed)."""
+        Q = np.empty(self.nq) if out is None else out
+        assert Q.dtype == np.float64 and Q.flags.c_contiguous and Q.size == self.nq
         check(self.L.chorus_gpu_download_state(self._ctx, _dp(Q)))
         return Q
 

@@ -63,6 +63,14 @@ static void make_ops(int N, const double* Lmat, const double* Mmat, const double
   for (int i = 0; i < (N + 1) * N; i++) { o.L[i] = Lmat[i]; o.M[i] = Mmat[i]; }
   for (int i = 0; i <= N; i++) o.Xf[i] = Xf[i];
   for (int i = 0; i < N; i++) o.Xs[i] = Xs[i];
+  for (int f = 0; f <= N / 2; f++) {
+    for (int j = 0; j < N / 2; j++) {
+      const double a = Lmat[f + (N + 1) * j], b = Lmat[f + (N + 1) * (N - 1 - j)];
+      o.CE[f * kHalfS + j] = 0.5 * (a + b);
+      o.CO[f * kHalfS + j] = 0.5 * (a - b);
+    }
+    o.LMID[f] = (N & 1) ? Lmat[f + (N + 1) * ((N - 1) / 2)] : 0.0;
+  }
   // AV smoothing A = Hlow * H: project N points onto the N-1 low-order points
   // (hhval at Xs_low, AV.f90:19-35) and evaluate back (hhval_low at Xs, :41-58)
   double xsl[kMaxN], xfl[kMaxN + 1];
@@ -119,10 +127,14 @@ static const Dispatch* dispatch_for(int N) {
 
 // default launch shapes per N (cells per CTA, threads per CTA)
 Launch default_launch(int N, int which) {
-  // which: 0 = E1, 1 = E2, 2 = E3, 3 = CT
-  static const int epb[kMaxN + 1][4] = {{0}, {0}, {16, 16, 16, 16}, {8, 8, 8, 8}, {8, 6, 8, 8},
-                                        {4, 4, 4, 4}, {4, 2, 4, 4}, {2, 2, 2, 2}, {2, 2, 2, 2}};
-  return Launch{epb[N][which], 128};
+  // which: 0 = E1, 1 = E2, 2 = E3, 3 = CT; cells per CTA and threads per CTA as the
+  // autotuner picked them on GB300 for N = 3..6 (the CT pass takes E3's shape)
+  static const int epb[kMaxN + 1][4] = {{0}, {0}, {16, 16, 16, 16}, {8, 16, 8, 8}, {4, 2, 4, 4},
+                                        {4, 1, 4, 4}, {4, 4, 2, 2}, {2, 2, 2, 2}, {2, 2, 2, 2}};
+  static const int thr[kMaxN + 1][4] = {{0}, {0}, {128, 128, 128, 128}, {256, 256, 128, 128}, {128, 64, 128, 128},
+                                        {256, 64, 128, 128}, {256, 256, 128, 128}, {128, 128, 128, 128},
+                                        {128, 128, 128, 128}};
+  return Launch{epb[N][which], thr[N][which]};
 }
 
 }  // namespace chorus
@@ -207,6 +219,14 @@ extern "C" {
 
 const char* chorus_gpu_last_error(void) { return g_err.c_str(); }
 const char* chorus_gpu_version(void) { return "chorus-gb300 0.1 (sm_103a, FP64)"; }
+
+int chorus_gpu_device_name(int32_t device, char* buf, int32_t n) {
+  if (!buf || n <= 0) return set_err(CHORUS_EINVAL, "null buffer");
+  cudaDeviceProp p;
+  CK(cudaGetDeviceProperties(&p, device));
+  std::snprintf(buf, (size_t)n, "%s", p.name);
+  return CHORUS_OK;
+}
 
 int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* IBFINTER, const int32_t* IBFREE,
                     const int32_t* CYC2FPAIR, const int32_t* iface2fp, const int32_t* jface2fp, const double* Xs,
@@ -358,7 +378,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
     const double mag = std::sqrt(n1 * n1 + n2 * n2);
     o.ux = n1 / mag * sign_l;
     o.uy = n2 / mag * sign_l;
-    o.msl = mag * sign_l;
+    o.msl = 0.5 * (mag * sign_l);  // the 1/2 of the Rusanov average folded in
     o.ss = (double)(sign_l * sign_r);
   };
   for (int f = 0; f < c->nface2; f++)

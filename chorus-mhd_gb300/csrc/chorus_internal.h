@@ -48,7 +48,7 @@ void initial_point(int problem, double gam, double x, double y, const double* B,
 //   Se         [e]           AV sensor sum of variable 1 (the reference's SM_IND(1) is log10 of it)
 //   muf        [e][4]        face-averaged AV viscosity per local face 1..4
 // ---------------------------------------------------------------------------
-struct FaceNorm {  // per two-sided face point: unit normal, magnorm*sign_l, sign_l*sign_r
+struct FaceNorm {  // per face point: unit normal, magnorm*sign_l/2, sign_l*sign_r (+-1)
   double ux, uy, msl, ss;
 };
 

@@ -28,12 +28,24 @@
 
 namespace chorus {
 
+constexpr int kHalfF = kMaxN / 2 + 1;  // flux points up to the middle of a line
+constexpr int kHalfS = kMaxN / 2;      // mirrored pairs of solution points
+
 struct OpsN {
   double L[(kMaxN + 1) * kMaxN];  // Lmat(N+1,N) column-major
   double M[(kMaxN + 1) * kMaxN];  // Mmat(N+1,N)
   double A[kMaxN * kMaxN];        // AV smoothing operator A[i*N+m] (projection to N-1 points and back)
   double Xf[kMaxN + 1];
   double Xs[kMaxN];
+  // Lmat split by the mirror symmetry of the points (Xs and Xf symmetric about 1/2):
+  // for flux point f <= N/2 and solution pair (j, N-1-j),
+  //   CE[f][j] = (L(f,j) + L(f,N-1-j))/2,  CO[f][j] = (L(f,j) - L(f,N-1-j))/2,
+  // LMID[f] = L(f,(N-1)/2) for odd N; then with e_j = q_j + q_{N-1-j},
+  // o_j = q_j - q_{N-1-j}: Qf(f) = E + O and Qf(N-f) = E - O,
+  // E = sum CE e + LMID q_mid, O = sum CO o.
+  double CE[kHalfF * kHalfS];
+  double CO[kHalfF * kHalfS];
+  double LMID[kHalfF];
 };
 
 // one copy per translation unit; upload_ops_n<N>() fills it
@@ -138,22 +150,40 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
     for (int i = threadIdx.x; i < N * N; i += blockDim.x) sA[i] = O::ops().A[i];
   }
   __syncthreads();
-  // interpolation to every flux point, one (cell, flux point, variable) per thread so
-  // that every lane of every warp does FP64 work
-  for (int t = threadIdx.x; t < cnt * NFP * 9; t += blockDim.x) {
-    const int k = t % 9, ef = t / 9, e = ef / NFP, fp = ef - e * NFP;
+  // interpolation to every flux point, one (cell, line, variable) per thread so that
+  // every lane of every warp does FP64 work; the mirror symmetry of the points halves
+  // the multiplications (see OpsN::CE)
+  for (int t = threadIdx.x; t < cnt * 2 * N * 9; t += blockDim.x) {
+    const int k = t % 9, el = t / 9, e = el / (2 * N), line = el - e * 2 * N;
     const double* q = sQ + e * NS * 9 + k;
-    double a = 0.0;
-    if (fp < NF1) {
-      const int ifp = fp % (N + 1), jfp = fp / (N + 1);
+    const bool fam1 = line < N;
+    const int ln = fam1 ? line : line - N;
+    // solution values along the line and where the line's flux values go
+    const double* qb = fam1 ? q + ln * N * 9 : q + ln * 9;
+    const int qs = fam1 ? 9 : N * 9;
+    double* ob = sV + (e * NFP + (fam1 ? ln * (N + 1) : NF1 + ln)) * 9 + k;
+    const int os = fam1 ? 9 : N * 9;
+    double v[N];
 #pragma unroll
-      for (int sp = 0; sp < N; sp++) a += q[(jfp * N + sp) * 9] * sL[ifp + (N + 1) * sp];
-    } else {
-      const int r = fp - NF1, ifp = r % N, jfp = r / N;
+    for (int sp = 0; sp < N; sp++) v[sp] = qb[sp * qs];
+    double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
 #pragma unroll
-      for (int sp = 0; sp < N; sp++) a += q[(sp * N + ifp) * 9] * sL[jfp + (N + 1) * sp];
+    for (int j = 0; j < N / 2; j++) {
+      ev[j] = v[j] + v[N - 1 - j];
+      od[j] = v[j] - v[N - 1 - j];
     }
-    sV[t] = a;
+#pragma unroll
+    for (int f = 0; f <= N / 2; f++) {
+      double E = (N & 1) ? O::ops().LMID[f] * v[(N - 1) / 2] : 0.0;
+      double Od = 0.0;
+#pragma unroll
+      for (int j = 0; j < N / 2; j++) {
+        E += O::ops().CE[f * kHalfS + j] * ev[j];
+        Od += O::ops().CO[f * kHalfS + j] * od[j];
+      }
+      ob[f * os] = E + Od;
+      if (f != N - f) ob[(N - f) * os] = E - Od;
+    }
   }
   __syncthreads();
   // contravariant inviscid flux at the interior flux points only
@@ -309,12 +339,12 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
       for (int k = 0; k < 9; k++) qr[k] = ql[k];
     }
     double Fh[8], vnl, ev;
-    rusanov_core(ql, qr, fn.ux, fn.uy, s.gam, Fh, vnl, ev);
+    rusanov_core(ql, qr, fn.ux, fn.uy, s.gam, fn.msl, Fh, vnl, ev);
     evb = ev_bits(ev, s.err);
     const double az = vnl > 0.0 ? ql[8] : qr[8];
     double* fl = s.Fc + gl * 8;
 #pragma unroll
-    for (int k = 0; k < 8; k++) fl[k] = fn.msl * Fh[k];
+    for (int k = 0; k < 8; k++) fl[k] = Fh[k];
     s.Azf[gl] = az;
     if (two && s.skip && nfp == 0) {
       const int4 fc = s.face2[f];
@@ -326,13 +356,13 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
     if (two) {
       double* fr = s.Fc + gr * 8;
 #pragma unroll
-      for (int k = 0; k < 8; k++) fr[k] = fn.ss * (fn.msl * Fh[k]);
+      for (int k = 0; k < 8; k++) fr[k] = times_sign(Fh[k], fn.ss);
       s.Azf[gr] = az;
       double* al = s.Qvf + gl * 9;
       double* ar = s.Qvf + gr * 9;
 #pragma unroll
       for (int k = 0; k < 9; k++) {
-        const double a = 0.5 * ql[k] + 0.5 * qr[k];
+        const double a = half(ql[k] + qr[k]);
         al[k] = a;
         ar[k] = a;
       }
@@ -356,14 +386,14 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
   __shared__ int list[64];
 
   double* sQ = sm;                  // [epb][NFP][9]
-  double* sA = sQ + epb * NFP * 9;  // [epb][NFP]
-  double* sG = sA + epb * NFP;      // [epb][NS][16]  (d*8 + k)
+  double* sG = sQ + epb * NFP * 9;  // [epb][NS][16]  (d*8 + k)
   double* sL = sG + epb * NS * 16;  // Lmat (N+1, N)
+  // grad A_z (nablaAsp) is computed with the divergence in the last pass; this pass
+  // only serves the cells whose gradients the viscous fluxes need
   const int nact = active_cells(s, e0, cnt, 0, list);
+  if (nact == 0) return;
   {
     for (int i = threadIdx.x; i < (N + 1) * N; i += blockDim.x) sL[i] = O::ops().L[i];
-    const double* ga = s.Azf + (size_t)e0 * NFP;
-    for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) sA[i] = ga[i];
     // flux-point states only for the cells whose gradients are needed
     for (int i = threadIdx.x; i < nact * NFP * 9; i += blockDim.x) {
       const int le = i / (NFP * 9), r = i - le * (NFP * 9), e = list[le];
@@ -371,25 +401,6 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
     }
   }
   __syncthreads();
-  // grad A_z at every solution point of every cell (nablaAsp)
-  for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
-    const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
-    const size_t gs = (size_t)(e0 + e) * NS + p;
-    const double* w = s.gco + (size_t)(e0 + e) * NG * NS + p;
-    const double* az = sA + e * NFP;
-    double ax = 0.0, ay = 0.0;
-#pragma unroll
-    for (int r = 0; r <= N; r++) {
-      const double a = az[js * (N + 1) + r];
-      const double b = az[NF1 + r * N + is];
-      ax += w[r * NS] * a;
-      ax += w[((N + 1) + r) * NS] * b;
-      ay += w[(2 * (N + 1) + r) * NS] * a;
-      ay += w[(3 * (N + 1) + r) * NS] * b;
-    }
-    s.nAs[2 * gs] = ax;
-    s.nAs[2 * gs + 1] = ay;
-  }
   // grad Q (variables 1-8) where needed (nablaQsp)
   for (int t = threadIdx.x; t < nact * NS; t += blockDim.x) {
     const int le = t / NS, p = t - le * NS, e = list[le], is = p % N, js = p / N;
@@ -488,7 +499,7 @@ __device__ __forceinline__ void f2_point(const SolveDev& s, int t) {
     for (int d = 0; d < 2 * live; d++)
 #pragma unroll
       for (int k = 0; k < 8; k++) {
-        const double v = 0.5 * a[9 * d + k] + 0.5 * b[9 * d + k];
+        const double v = half(a[9 * d + k] + b[9 * d + k]);
         a[9 * d + k] = v;
         b[9 * d + k] = v;
       }
@@ -523,15 +534,26 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
   double* sD = sF + epb * NFP * 8;  // [epb][NS] diagnostic partial sums
   double* sQ = sD + epb * NS;       // [epb][NS][9] state of the block's cells
   double* sR = sQ + epb * NS * 9;   // [epb][NS][9] residual
-  double* sM = sR + epb * NS * 9;   // Mmat (N+1, N)
+  double* sJ = sR + epb * NS * 9;   // [epb][NS] 1/J
+  double* sZ = sJ + epb * NS;       // [epb][NFP][2] A_z * (S_x, S_y) at the flux points
+  double* sN = sZ + epb * NFP * 2;  // [epb][NS][2] grad A_z
+  double* sM = sN + epb * NS * 2;   // Mmat (N+1, N)
   __shared__ int list[64];
   const int nact = active_cells(s, e0, cnt, 1, list);
   {
-    // every global access of the pass is a contiguous block copy (coalesced)
+    // every global access of the pass is a contiguous block copy (coalesced), issued
+    // together so their latencies overlap
     const double* fi = s.Fc + (size_t)e0 * NFP * 8;
     for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) sF[i] = -fi[i];
-    const double* gq = s.Q + (size_t)e0 * NS * 9;
-    for (int i = threadIdx.x; i < cnt * NS * 9; i += blockDim.x) sQ[i] = gq[i];
+    const size_t q0 = (size_t)e0 * NS * 9;
+    for (int i = threadIdx.x; i < cnt * NS * 9; i += blockDim.x) sQ[i] = s.Q[q0 + i];
+    for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sJ[i] = s.invJ[(size_t)e0 * NS + i];
+    for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
+      const size_t g = (size_t)e0 * NFP + i;
+      const double z = s.Azf[g];
+      sZ[2 * i] = z * s.met[2 * g];
+      sZ[2 * i + 1] = z * s.met[2 * g + 1];
+    }
     for (int i = threadIdx.x; i < (N + 1) * N; i += blockDim.x) sM[i] = O::ops().M[i];
   }
   __syncthreads();
@@ -570,25 +592,42 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
     }
   }
   __syncthreads();
-  // divergence of the total flux, one (cell, point, variable) per thread
-  for (int t = threadIdx.x; t < cnt * NS * 8; t += blockDim.x) {
-    const int k = t % 8, ep = t / 8, e = ep / NS, p = ep - e * NS, is = p % N, js = p / N;
-    const double* Fe = sF + e * NFP * 8 + k;
+  // divergence of the total flux, one (cell, point, variable) per thread, then grad
+  // A_z in the conservative form of nablaAsp (magnetic_potential.f90:1-42),
+  // (1/J) sum_r Mmat (A_z S) over both line families, one (cell, point, component) per
+  // thread; 2(N+1) FMAs per item either way, and the two ranges split between warps
+  // (only the warp that straddles them diverges)
+  const int ndiv = cnt * NS * 8;
+  for (int t = threadIdx.x; t < ndiv + cnt * NS * 2; t += blockDim.x) {
     double a = 0.0;
+    if (t < ndiv) {
+      const int k = t & 7, ep = t >> 3, e = ep / NS, p = ep - e * NS, is = p % N, js = p / N;
+      const double* Fe = sF + e * NFP * 8 + k;
 #pragma unroll
-    for (int r = 0; r <= N; r++) {
-      a += sM[r + (N + 1) * is] * Fe[(js * (N + 1) + r) * 8];
-      a += sM[r + (N + 1) * js] * Fe[(NF1 + r * N + is) * 8];
+      for (int r = 0; r <= N; r++) {
+        a += sM[r + (N + 1) * is] * Fe[(js * (N + 1) + r) * 8];
+        a += sM[r + (N + 1) * js] * Fe[(NF1 + r * N + is) * 8];
+      }
+      sR[ep * 9 + k] = a * sJ[ep];
+    } else {
+      const int u = t - ndiv, c = u & 1, ep = u >> 1, e = ep / NS, p = ep - e * NS, is = p % N, js = p / N;
+      const double* az = sZ + e * NFP * 2 + c;
+#pragma unroll
+      for (int r = 0; r <= N; r++) {
+        a += sM[r + (N + 1) * is] * az[(js * (N + 1) + r) * 2];
+        a += sM[r + (N + 1) * js] * az[(NF1 + r * N + is) * 2];
+      }
+      a *= sJ[ep];
+      sN[u] = a;
+      s.nAs[(size_t)e0 * NS * 2 + u] = a;
     }
-    sR[ep * 9 + k] = a * s.invJ[(size_t)(e0 + e) * NS + p];
   }
+  __syncthreads();
   // A_z advection (resid(9), compresid.f90:45-47) at every solution point
   for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
-    const int e = t / NS, p = t - e * NS;
-    const size_t gs = (size_t)(e0 + e) * NS + p;
     const double* q = sQ + t * 9;
     const double ri = rcp_pos(q[0]);
-    const double ax = s.nAs[2 * gs] - s.B0y, ay = s.nAs[2 * gs + 1] + s.B0x;
+    const double ax = sN[2 * t] - s.B0y, ay = sN[2 * t + 1] + s.B0x;
     sR[t * 9 + 8] = -(q[1] * ri * ax + q[2] * ri * ay);
   }
   if (rk.diag) {
@@ -711,7 +750,7 @@ __device__ __forceinline__ void ctface_point(const SolveDev& s, int t) {
   const int4 fc = s.face2[f];
   const size_t gl = (size_t)fc.x * NFP + face_fp<N>(fc.y, nfp);
   const size_t gr = (size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp);
-  const double v = 0.5 * s.Qvf[gl * 9 + 8] + 0.5 * s.Qvf[gr * 9 + 8];
+  const double v = half(s.Qvf[gl * 9 + 8] + s.Qvf[gr * 9 + 8]);
   s.Qvf[gl * 9 + 8] = v;
   s.Qvf[gr * 9 + 8] = v;
 }

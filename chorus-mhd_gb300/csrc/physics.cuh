@@ -29,6 +29,28 @@ __host__ __device__ __forceinline__ double rcp_pos(double x) {
 #endif
 }
 
+// x/2 without an FP64 instruction: decrement the exponent field (exact for normal
+// numbers, the same value as 0.5*x); zeros, subnormals, infinities and NaNs take the
+// multiply.  0.5*a + 0.5*b == half(a + b) bit for bit for normal operands.
+__host__ __device__ __forceinline__ double half(double x) {
+#ifdef __CUDA_ARCH__
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  return (ex > 1 && ex < 0x7FF) ? __longlong_as_double(b - (1LL << 52)) : 0.5 * x;
+#else
+  return 0.5 * x;
+#endif
+}
+
+// x * s for s = +-1 as a sign-bit flip (integer pipe, exact)
+__host__ __device__ __forceinline__ double times_sign(double x, double s) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(__double_as_longlong(x) ^ (__double_as_longlong(s) & (long long)0x8000000000000000ULL));
+#else
+  return x * s;
+#endif
+}
+
 // Contravariant ideal-MHD flux F*sx + G*sy of getIfluxvectors (getrusanov.f90:111-153)
 // as used by inviscid_flux_interior (compflux.f90:77-78, 96-97).
 __host__ __device__ __forceinline__ void iflux_contra(const double* q, double sx, double sy, double gm1,
@@ -52,12 +74,14 @@ __host__ __device__ __forceinline__ void iflux_contra(const double* q, double sx
   F[7] = Bz * Un - w * Bn;
 }
 
-// Rusanov flux of getrusanovflux (getrusanov.f90:1-109) before the transform to the
-// computational frame: Fh = 0.5*(Fl + Fr - eigv*(qr - ql)) along the unit normal
-// (ux,uy); returns the left normal velocity (for the A_z upwinding, :99-103) and the
-// wave-speed bound eigv (:87).
+// Rusanov flux of getrusanovflux (getrusanov.f90:1-109) along the unit normal (ux,uy),
+// times `scale`: Fh = scale*(Fl + Fr - eigv*(qr - ql)); with scale = magnorm*sign_l/2
+// this is the reference's Fnl in the left cell's computational frame (:90-93).  Returns
+// the left normal velocity (for the A_z upwinding, :99-103) and the wave-speed bound
+// eigv (:87).
 __host__ __device__ __forceinline__ void rusanov_core(const double* ql, const double* qr, double ux, double uy,
-                                                      double gam, double* Fh, double& vnl, double& eigv) {
+                                                      double gam, double scale, double* Fh, double& vnl,
+                                                      double& eigv) {
   const double gm1 = gam - 1.0;
   double Fl[8], Fr[8], pgl, pgr, vn[2];
   const double* qs[2] = {ql, qr};
@@ -97,7 +121,7 @@ __host__ __device__ __forceinline__ void rusanov_core(const double* ql, const do
   const double cf = sqrt(0.5 * (cad + ctmp));
   eigv = 0.5 * fabs(vn[0] + vn[1]) + cf;
 #pragma unroll
-  for (int k = 0; k < 8; k++) Fh[k] = 0.5 * (Fl[k] + Fr[k] - eigv * (qr[k] - ql[k]));
+  for (int k = 0; k < 8; k++) Fh[k] = scale * fma(-eigv, qr[k] - ql[k], Fl[k] + Fr[k]);
   vnl = vn[0];
 }
 

@@ -19,11 +19,11 @@ __global__ void k_point_rusanov(int n, double gam, const double* Qfl, const doub
   const double ux = n1 / mag * sign_l, uy = n2 / mag * sign_l;
   double ql[9], qr[9], Fh[8], vnl, e;
   for (int k = 0; k < 9; k++) { ql[k] = Qfl[9 * i + k]; qr[k] = Qfr[9 * i + k]; }
-  rusanov_core(ql, qr, ux, uy, gam, Fh, vnl, e);
   const double msl = mag * sign_l, ss = (double)(sign_l * sign_r);
+  rusanov_core(ql, qr, ux, uy, gam, 0.5 * msl, Fh, vnl, e);
   for (int k = 0; k < 8; k++) {
-    Fnl[8 * i + k] = msl * Fh[k];
-    Fnr[8 * i + k] = ss * (msl * Fh[k]);
+    Fnl[8 * i + k] = Fh[k];
+    Fnr[8 * i + k] = times_sign(Fh[k], ss);
   }
   Az[i] = vnl > 0.0 ? ql[8] : qr[8];
   ev[i] = e;

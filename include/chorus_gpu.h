@@ -75,6 +75,8 @@ typedef struct ChorusBatch ChorusBatch;
 const char* chorus_gpu_last_error(void);
 /* Library version string. */
 const char* chorus_gpu_version(void);
+/* Name of a CUDA device (the key of the autotuned launch-shape tables). */
+int chorus_gpu_device_name(int32_t device, char* buf, int32_t n);
 
 /* ------------------------------------------------------------------------------
  * Binding (replaces the module state set up by INIT_SETUP, initsetup.f90:1-165)
