@@ -47,7 +47,7 @@ def workload_name():
 
 METRIC = "DOF*RK-stage/s"
 HBM_FALLBACK = 6800.0
-FP64_PEAK_TFLOPS = 1.20  # measured DFMA microbenchmark on this machine's GB300 (600 G DFMA/s)
+FP64_PEAK_GOPS = 600.0  # measured DFMA-chain microbenchmark on this GB300: 600 G FMA/s (1.20 TFLOP/s)
 
 
 def b_stage(N: int) -> float:
@@ -190,12 +190,19 @@ def run_gpu(args):
     hbm_peak, peak_kind = measured_peaks()
     stage_ms = prof[5]
     achieved = b_stage(N) * nc / (stage_ms / 1e3) / 1e9
-    flops_es = FLOPS_PER_ELEMENT_STAGE.get(N)
+    ops = FP64_PER_ELEMENT_STAGE.get(N)
     fp64 = None
-    if flops_es:
-        tf = flops_es * nc / (stage_ms / 1e3) / 1e12
-        fp64 = {"achieved_tflops": tf, "peak_tflops": FP64_PEAK_TFLOPS, "frac": tf / FP64_PEAK_TFLOPS,
-                "flops_per_element_stage": flops_es, "source": "ncu sass op counts, profiles/"}
+    if ops:
+        n_ops, n_flops = ops
+        gops = n_ops * nc / (stage_ms / 1e3) / 1e9
+        fp64 = {"bound": "fp64 pipe", "achieved_gops": gops, "peak_gops": FP64_PEAK_GOPS,
+                "frac": gops / FP64_PEAK_GOPS, "unit": "G FP64 instructions/s (thread level)",
+                "ops_per_element_stage": n_ops, "flops_per_element_stage": n_flops,
+                "achieved_tflops": n_flops * nc / (stage_ms / 1e3) / 1e12,
+                "source": "ncu SASS counters of the five stage kernels, Orszag-Tang 192x192 N=5"}
+    traffic = None
+    if TRAFFIC_PER_ELEMENT_STAGE.get(N):
+        traffic = TRAFFIC_PER_ELEMENT_STAGE[N] * nc
 
     # end to end through the C-ABI with host buffers: H2D of Q, one step, D2H of Q
     pinned = torch.empty(sol.nq, dtype=torch.float64, pin_memory=True)
@@ -236,7 +243,9 @@ def run_gpu(args):
         "e2e": e2e,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": TRAFFIC_PER_STAGE.get(N),
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the five stage "
+                                       "kernels at 192x192, scaled by cells (bytes per cell are size-independent)",
                      "kernel": "one RK stage (5 launches: %s)" % ", ".join(names),
                      "algorithmic_bytes_per_element_stage": b_stage(N), "peak_kind": peak_kind,
                      "stage_ms": stage_ms, "dominant_kernel": names[dom],
@@ -343,10 +352,11 @@ def run_serving(args, device, tmp):
     return out
 
 
-# FP64 flops per element per stage (2*DFMA + DADD + DMUL, from ncu SASS counters on
-# the stage kernels; see profiles/) and DRAM bytes per stage (ncu, scaled to 512^2)
-FLOPS_PER_ELEMENT_STAGE: dict = {}
-TRAFFIC_PER_STAGE: dict = {}
+# per element per RK stage, from ncu on the five stage kernels (Orszag-Tang 192x192,
+# N=5, after the warm-up steps): FP64 thread instructions (DFMA + DADD + DMUL) and flops
+# (2*DFMA + DADD + DMUL); DRAM bytes read + written
+FP64_PER_ELEMENT_STAGE: dict = {}
+TRAFFIC_PER_ELEMENT_STAGE: dict = {}
 
 
 def cpu_baseline(case_dir, dof, warm=1, timed=2):

@@ -7,6 +7,6 @@ synthetic-case writer ``meshgen``.
 """
 from . import meshgen  # noqa: F401
 from ._lib import ChorusError, load  # noqa: F401
-from .solver import Mesh, Solver, reference_layout_sizes  # noqa: F401
+from .solver import Mesh, Plot, Solver, plot_filename, reference_layout_sizes  # noqa: F401
 from .batch import Batch  # noqa: F401
 from . import serve  # noqa: F401

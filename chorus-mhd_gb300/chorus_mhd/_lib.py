@@ -70,6 +70,7 @@ SIGNATURES = {
     "getrusanovflux_noalloc_gpu": (c_int, [c_int, c_double, dp, dp, dp, dp, dp, dp, ip, ip, dp]),
     "getifluxvectors_gpu": (c_int, [c_int, c_double, dp, dp, dp]),
     "getvfluxvectors_gpu": (c_int, [c_int, c_double, c_double, c_double, dp, dp, dp, dp]),
+    "getvfluxvectors_av_gpu": (c_int, [c_void_p, c_int, dp, dp, dp, dp, ip, ip, ip, ip]),
     "chorus_gpu_stream": (c_void_p, [c_void_p]),
     "chorus_gpu_set_option": (c_int, [c_void_p, c_char_p, ctypes.c_int64]),
     "chorus_gpu_get_option": (ctypes.c_int64, [c_void_p, c_char_p]),
@@ -88,6 +89,14 @@ SIGNATURES = {
     "chorus_mesh_device_bytes": (ctypes.c_int64, [c_void_p]),
     "chorus_mesh_load": (c_int, [c_char_p, P(c_void_p)]),
     "chorus_mesh_free": (c_int, [c_void_p]),
+    "chorus_mesh_output_info": (c_int, [c_void_p, ip, ip]),
+    "chorus_plot_create": (c_int, [c_void_p, ip, ip, dp, dp, c_int, c_int, dp, c_int, P(c_void_p)]),
+    "chorus_plot_create_mesh": (c_int, [c_void_p, c_void_p, c_int, P(c_void_p)]),
+    "chorus_plot_free": (c_int, [c_void_p]),
+    "chorus_plot_info": (c_int, [c_void_p, P(ctypes.c_int64), P(ctypes.c_int64), ip]),
+    "chorus_plot_values": (c_int, [c_void_p, dp, dp, dp, ip, ip]),
+    "chorus_plot_filename": (c_int, [c_double, c_char_p, c_int]),
+    "chorus_plot_write": (c_int, [c_void_p, c_double, c_char_p, c_char_p, c_int]),
     "chorus_mesh_info": (c_int, [c_void_p, P(ChorusDims), P(ChorusParams), ip, ip]),
     "chorus_mesh_iarray": (ip, [c_void_p, c_char_p, P(ctypes.c_int64)]),
     "chorus_mesh_darray": (dp, [c_void_p, c_char_p, P(ctypes.c_int64)]),

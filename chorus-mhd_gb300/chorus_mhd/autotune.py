@@ -36,7 +36,7 @@ def cache_path(gpu_name: str) -> str:
 def _smem_bytes(N: int, pass_: str, epb: int) -> int:
     NS, NFP = N * N, 2 * (N + 1) * N
     per = {"e1": NS * 9 + 2 * NS + NFP * 18, "e2": NFP * 9 + NS * 16,
-           "e3": NFP * 10 + NS * 22, "ct": NFP}[pass_]
+           "e3": NFP * 10 + NS * 13, "ct": NFP}[pass_]
     return 8 * (epb * per + 2 * (N + 1) * N)
 
 

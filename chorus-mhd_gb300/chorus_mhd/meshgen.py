@@ -57,6 +57,7 @@ class CaseSpec:
     eta0: float = 0.0
     artiv: int = 1
     nwrite: int = 1000000
+    nre: int = 1                    # plot sub-intervals per cell edge (readinput.f90:32)
     gamma: float | None = None      # None: the problem's default
     extra: dict = field(default_factory=dict)
 
@@ -216,7 +217,7 @@ def write_case(spec: CaseSpec, out_dir: str, name: str = "mesh") -> str:
         "artificial viscosity",
         "%d" % spec.artiv,
         "output",
-        "1",
+        "%d" % spec.nre,
         "%d" % spec.nwrite,
         "restart",
         "0",

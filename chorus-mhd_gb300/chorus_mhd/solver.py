@@ -10,6 +10,7 @@ flattened (first index fastest).
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -40,6 +41,9 @@ class Mesh:
         check(self.L.chorus_mesh_info(self._h, ctypes.byref(self.dims), ctypes.byref(self.params),
                                       ctypes.byref(mi), ctypes.byref(pb)))
         self.maxiter, self.problem = mi.value, pb.value
+        nre, nw = ctypes.c_int32(), ctypes.c_int32()
+        check(self.L.chorus_mesh_output_info(self._h, ctypes.byref(nre), ctypes.byref(nw)))
+        self.nre, self.nwrite = nre.value, nw.value
 
     @property
     def N(self):
@@ -73,6 +77,54 @@ class Mesh:
             self.close()
         except Exception:
             pass
+
+
+class Plot:
+    """Plot output of one solve (tecplotter2dsetup / tecplotter2d / tecpost_parallel):
+    the plot-node topology is built once; values() evaluates the nodes on the device,
+    write() also writes the reference's Tecplot binary file."""
+
+    def __init__(self, solver: "Solver", nre: int = 0):
+        self.L = solver.L
+        self.solver = solver
+        h = ctypes.c_void_p()
+        check(self.L.chorus_plot_create_mesh(solver._ctx, solver.mesh._h, int(nre), ctypes.byref(h)))
+        self._h = h
+        n, c, w = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
+        check(self.L.chorus_plot_info(self._h, ctypes.byref(n), ctypes.byref(c), ctypes.byref(w)))
+        self.nodes, self.cells, self.warned = n.value, c.value, bool(w.value)
+
+    def values(self) -> dict:
+        X = np.empty(2 * self.nodes)
+        Q = np.empty(9 * self.nodes)
+        AV = np.empty(2 * self.nodes)
+        con = np.empty(4 * self.cells, np.int32)
+        fac = np.empty(self.nodes, np.int32)
+        check(self.L.chorus_plot_values(self._h, _dp(X), _dp(Q), _dp(AV), _ip(con), _ip(fac)))
+        return dict(plotX=X, plotQ=Q, plotAV=AV, connec_c2n=con, gnode_factor=fac)
+
+    def write(self, directory: str, ctime: float | None = None) -> str:
+        out = ctypes.create_string_buffer(4096)
+        t = self.solver.ctime if ctime is None else float(ctime)
+        check(self.L.chorus_plot_write(self._h, t, directory.encode(), out, 4096))
+        return out.value.decode()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.chorus_plot_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def plot_filename(ctime: float) -> str:
+    buf = ctypes.create_string_buffer(64)
+    check(_lib.load().chorus_plot_filename(float(ctime), buf, 64))
+    return buf.value.decode()
 
 
 def device_name(device: int = 0) -> str:
@@ -179,6 +231,37 @@ class Solver:
                     eigvmax_g=r.eigvmax_g, epsilon0=r.epsilon0) for r in recs[: min(nd.value, cap)]]
         self.diagnostics.extend(out)
         return out
+
+    def run(self, maxiter: int | None = None, out_dir: str | None = None, nwrite: int | None = None,
+            nre: int = 0) -> list[dict]:
+        """The iteration loop of iterations.f90:19-87 up to MAXITER, with its output
+        schedule (:80-84): after step iter, when mod(iter, nwrite) == 1 or iter >=
+        MAXITER, the Tecplot file and the restart file restart.<iter %08d>.dat
+        (write_data.f90:44) go to out_dir (no output when out_dir is None)."""
+        maxiter = self.mesh.maxiter if maxiter is None else int(maxiter)
+        nwrite = self.mesh.nwrite if nwrite is None else int(nwrite)
+        plot = Plot(self, nre) if out_dir else None
+        recs = []
+        try:
+            while self.iter < maxiter:
+                nxt = maxiter
+                if out_dir and nwrite > 1:
+                    # next iter with mod(iter, nwrite) == 1
+                    k = self.iter + 1
+                    r = (1 - k) % nwrite
+                    nxt = min(maxiter, k + r)
+                recs += self.iterations(nxt - self.iter)
+                if out_dir and ((nwrite > 1 and self.iter % nwrite == 1) or self.iter >= maxiter):
+                    plot.write(out_dir)
+                    self.write_restart(os.path.join(out_dir, "restart.%08d.dat" % self.iter))
+        finally:
+            if plot:
+                plot.close()
+        return recs
+
+    def plot(self, nre: int = 0) -> "Plot":
+        """Plot output object for this solve (NRE from the case file when nre <= 0)."""
+        return Plot(self, nre)
 
     # ---- runtime helpers
     def set_option(self, name: str, value: int):

@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(128) kb_e1(BatchDev b, int slot, int sensor_on
   for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
     const int4 T = b.ctiles[ti];
     const SolveDev& s = load_solve(b.solves + T.x);
-    const int sensor = sensor_on ? s.artiv : 0;
+    const int sensor = s.artiv ? sensor_on : 0;  // 1: variable-1 sensor; 3: also variable 6
 #define CALL(n) e1_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sensor, sm)
     CHORUS_BATCH_SWITCH(T.w, CALL)
 #undef CALL
@@ -164,7 +164,7 @@ size_t cell_smem_bytes(int N, int epb) {
   const int NS = N * N, NFP = 2 * (N + 1) * N;
   size_t e1 = (size_t)epb * (NS * 9 + 2 * NS + NFP * 18) + (N + 1) * N + N * N;
   size_t e2 = (size_t)epb * (NFP * 9 + NS * 16) + (N + 1) * N;
-  size_t e3 = (size_t)epb * (NFP * 8 + NS * (1 + 9 + 9 + 1 + 2) + NFP * 2) + (N + 1) * N;
+  size_t e3 = (size_t)epb * (NFP * 8 + NS * (1 + 9 + 1 + 2) + NFP * 2) + (N + 1) * N;
   size_t ct = (size_t)epb * NFP;
   return sizeof(double) * std::max(std::max(e1, e2), std::max(e3, ct));
 }
@@ -339,7 +339,7 @@ static void batch_enqueue_step(ChorusBatch* b) {
   for (int stage = 0; stage < 5; stage++) {
     cudaMemsetAsync(b->d_counters, 0, sizeof(int) * kCounterSlots, b->st);
     cudaMemsetAsync(b->d_eig, 0, sizeof(unsigned long long) * 2 * b->cap_solves, b->st);
-    kb_e1<<<b->grid_cells, 128, sm, b->st>>>(a, 0, 1);
+    kb_e1<<<b->grid_cells, 128, sm, b->st>>>(a, 0, stage == 4 ? 3 : 1);
     kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 1, 0);
     kb_e2<<<b->grid_cells, 128, sm, b->st>>>(a, 2);
     kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 3, 1);

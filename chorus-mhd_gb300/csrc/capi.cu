@@ -107,7 +107,7 @@ static int ensure_ops(int dev, int N, const double* Lmat, const double* Mmat, co
 // per-N dispatch of the stage launches
 // ---------------------------------------------------------------------------
 struct Dispatch {
-  void (*e1)(const SolveDev&, const Launch&, cudaStream_t);
+  void (*e1)(const SolveDev&, const Launch&, cudaStream_t, int);
   void (*e1ns)(const SolveDev&, const Launch&, cudaStream_t);
   void (*f1)(const SolveDev&, cudaStream_t);
   void (*e2)(const SolveDev&, const Launch&, cudaStream_t);
@@ -208,7 +208,7 @@ static size_t arena_plan_bytes(int N, int NC, int nface2, int nface1, int k_stag
   P.take<double>(nq); P.take<double>(nfp * 9); P.take<double>(nfp * 8); P.take<double>(nfp);
   P.take<double>((size_t)NC * NS * 18); P.take<double>(nfp * 18); P.take<double>((size_t)NC * NS * 2);
   P.take<double>(nfp * 2); P.take<double>((size_t)NC * NS * NG); P.take<double>((size_t)NC * NS);
-  P.take<double>(NC); P.take<double>((size_t)NC * 4); P.take<double>((size_t)NC * 2);
+  P.take<double>((size_t)NC * 2); P.take<double>((size_t)NC * 4); P.take<double>((size_t)NC * 2);
   P.take<int4>(nface2 + 1); P.take<int2>(nface1 + 1); P.take<FaceNorm>((size_t)nface2 * N + 1);
   P.take<FaceNorm>((size_t)nface1 * N + 1); P.take<unsigned long long>(4); P.take<unsigned int>(4);
   P.take<double>(8); P.take<int>(NC); P.take<int>(NC); P.take<int4>(NC);
@@ -396,7 +396,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
          oAzf = P.take<double>(nfp), onQs = P.take<double>((size_t)NC * NS * 18), onQvf = P.take<double>(nfp * 18),
          onAs = P.take<double>((size_t)NC * NS * 2), omet = P.take<double>(nfp * 2),
          ogco = P.take<double>((size_t)NC * NS * NG), oinvJ = P.take<double>((size_t)NC * NS),
-         oSe = P.take<double>(NC), omuf = P.take<double>((size_t)NC * 4), odiag = P.take<double>((size_t)NC * 2),
+         oSe = P.take<double>((size_t)NC * 2), omuf = P.take<double>((size_t)NC * 4), odiag = P.take<double>((size_t)NC * 2),
          of2 = P.take<int4>(f2.size() + 1), of1 = P.take<int2>(f1.size() + 1),
          ofn2 = P.take<FaceNorm>(fn2.size() + 1), ofn1 = P.take<FaceNorm>(fn1.size() + 1),
          oeig = P.take<unsigned long long>(4), oerr = P.take<unsigned int>(4), ored = P.take<double>(8),
@@ -437,6 +437,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   s.gco = (const double*)(A + ogco);
   s.invJ = (const double*)(A + oinvJ);
   s.Se = (double*)(A + oSe);
+  s.Se6 = s.Se + NC;
   s.muf = (double*)(A + omuf);
   s.diag = (double*)(A + odiag);
   s.face2 = (const int4*)(A + of2);
@@ -578,10 +579,12 @@ int chorus_gpu_download_state(ChorusCtx* c, double* Q) {
 // ---------------------------------------------------------------------------
 namespace {
 
-void enqueue_stage(ChorusCtx* c, const RKStage& rk) {
+// one residual evaluation and stage update; `last` marks the last stage of a step (or a
+// single compresid), whose E1 also records the variable-6 sensor the plot output reads
+void enqueue_stage(ChorusCtx* c, const RKStage& rk, bool last) {
   const SolveDev& s = c->sd;
   cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st);
-  c->D->e1(s, c->L[0], c->st);
+  c->D->e1(s, c->L[0], c->st, last ? 1 : 0);
   c->D->f1(s, c->st);
   c->D->e2(s, c->L[1], c->st);
   c->D->f2(s, c->st);
@@ -632,7 +635,7 @@ void enqueue_rk(ChorusCtx* c, bool diag) {
   }
   r[4].diag = diag ? 1 : 0;
   r[4].write_resid = 1;  // the last stage's residual stays available like the reference's resid
-  for (int k = 0; k < 5; k++) enqueue_stage(c, r[k]);
+  for (int k = 0; k < 5; k++) enqueue_stage(c, r[k], k == 4);
 }
 
 __global__ void k_store_record(const double* red2, const unsigned long long* eig, double* rec) {
@@ -697,7 +700,7 @@ int compresid_gpu(ChorusCtx* c) {
   if (ctx_device(c)) return CHORUS_ECUDA;
   RKStage r = rk_blank();
   r.write_resid = 1;
-  enqueue_stage(c, r);
+  enqueue_stage(c, r, true);
   CK(cudaGetLastError());
   return check_err_flag(c);
 }
@@ -829,7 +832,7 @@ int chorus_gpu_profile_stage(ChorusCtx* c, int32_t reps, double* ms) {
   for (int it = 0; it < reps; it++) {
     CK(cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st));
     CK(cudaEventRecord(ev[0], c->st));
-    c->D->e1(s, c->L[0], c->st);
+    c->D->e1(s, c->L[0], c->st, 0);
     CK(cudaEventRecord(ev[1], c->st));
     c->D->f1(s, c->st);
     CK(cudaEventRecord(ev[2], c->st));
@@ -1000,6 +1003,42 @@ int getvfluxvectors_gpu(int32_t n, double gam, double mu, double eta0, const dou
   return CHORUS_OK;
 }
 
+int getvfluxvectors_av_gpu(ChorusCtx* c, int32_t n, const double* Qv, const double* nablaQ, double* Fv, double* Gv,
+                           const int32_t* fam, const int32_t* ifp, const int32_t* jfp, const int32_t* ic) {
+  if (!c) return set_err(CHORUS_EINVAL, "null context");
+  if (n < 0 || (n > 0 && (!Qv || !nablaQ || !Fv || !Gv || !fam || !ifp || !jfp || !ic)))
+    return set_err(CHORUS_EINVAL, "bad argument");
+  if (n == 0) return CHORUS_OK;
+  const int N = c->dims.N, NC = c->dims.NCELL;
+  for (int i = 0; i < n; i++) {
+    const int f = fam[i], ni = f == 1 ? N + 1 : N, nj = f == 1 ? N : N + 1;
+    if ((f != 1 && f != 2) || ifp[i] < 1 || ifp[i] > ni || jfp[i] < 1 || jfp[i] > nj || ic[i] < 1 || ic[i] > NC)
+      return set_err(CHORUS_EINVAL, "point %d: (fam, ifp, jfp, ic) = (%d, %d, %d, %d) out of range", i, f, ifp[i],
+                     jfp[i], ic[i]);
+  }
+  int rc = ctx_device(c);
+  if (rc) return rc;
+  PointAxes ax{};
+  for (int k = 0; k <= N; k++) ax.Xf[k] = c->Xf[k];
+  double *q, *g, *f, *h;
+  int *dfam, *di, *dj, *dc;
+  cudaStream_t st = c->st;  // ordered after the context's own work (muf of the last stage)
+  if (dev_copy(&q, Qv, 9 * (size_t)n, st) || dev_copy(&g, nablaQ, 18 * (size_t)n, st) ||
+      dev_copy<double>(&f, nullptr, 9 * (size_t)n, st) || dev_copy<double>(&h, nullptr, 9 * (size_t)n, st) ||
+      dev_copy(&dfam, fam, (size_t)n, st) || dev_copy(&di, ifp, (size_t)n, st) || dev_copy(&dj, jfp, (size_t)n, st) ||
+      dev_copy(&dc, ic, (size_t)n, st))
+    return CHORUS_ECUDA;
+  launch_point_vflux_av(n, c->p.gam, ax, c->sd.muf, dfam, di, dj, dc, q, g, f, h, st);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemcpy(Fv, f, 9 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(Gv, h, 9 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(q); cudaFree(g); cudaFree(f); cudaFree(h);
+  cudaFree(dfam); cudaFree(di); cudaFree(dj); cudaFree(dc);
+  if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "getvfluxvectors_av_gpu: %s", cudaGetErrorString(e));
+  return CHORUS_OK;
+}
+
 // ---------------------------------------------------------------------------
 // host-side setup
 // ---------------------------------------------------------------------------
@@ -1019,6 +1058,22 @@ int chorus_mesh_load(const char* dir, ChorusMesh** out) {
   }
   *out = mh;
   return CHORUS_OK;
+}
+
+int chorus_mesh_output_info(const ChorusMesh* mh, int32_t* nre, int32_t* nwrite) {
+  if (!mh) return set_err(CHORUS_EINVAL, "null mesh");
+  if (nre) *nre = mh->m.nre;
+  if (nwrite) *nwrite = mh->m.nwrite;
+  return CHORUS_OK;
+}
+
+int chorus_plot_create_mesh(ChorusCtx* ctx, const ChorusMesh* mh, int32_t NRE, ChorusPlot** plot) {
+  if (!mh) return set_err(CHORUS_EINVAL, "null mesh");
+  const Mesh& m = mh->m;
+  if (!ctx || ctx->dims.NCELL != m.NCELL || ctx->dims.N != m.N)
+    return set_err(CHORUS_EINVAL, "context and mesh differ");
+  return chorus_plot_create(ctx, m.IVCELL.data(), m.IC2F.data(), m.XV.data(), m.YV.data(), m.NVERT, m.NFACE,
+                            m.Xs.data(), NRE > 0 ? NRE : m.nre, plot);
 }
 
 int chorus_mesh_free(ChorusMesh* mh) {

@@ -18,6 +18,7 @@ constexpr int kMinN = 2;
 struct Mesh {
   int N = 0, NCELL = 0, NVERT = 0, NFACE = 0, NPAIR = 0;
   int maxiter = 0, problem = 0, restart = 0;
+  int nre = 1, nwrite = 0;  // plot sub-intervals per cell edge, output interval
   ChorusParams params{};
   std::vector<int32_t> IVCELL, IC2F, IF2C, IF2V, IBFINTER, IBFREE, IBFCYC, IBFCYCLOC, CYC2FPAIR;
   std::vector<int32_t> iface2fp, jface2fp;
@@ -75,6 +76,7 @@ struct SolveDev {
   const double* gco;
   const double* invJ;
   double* Se;
+  double* Se6;                  // the same sum for variable 6 (last stage only; plot output)
   double* muf;
   const int4* face2;            // (cL, lfL, cR, lfR): cells 0-based, local faces 1..4
   const FaceNorm* fn2;          // [face][nfp]
@@ -91,6 +93,7 @@ struct SolveDev {
   unsigned long long* eig;      // bit pattern of the stage's max wave speed (>= 0)
   unsigned int* err;            // error flags (bit 0: non-finite wave speed)
   double* diag;                 // per-cell diagnostic partial sums [e][2]
+  void* pad2;                   // keeps the size a multiple of 16 bytes
 };
 
 // One RK stage update: Qnew = sum_j c[j]*src[j] + cQ*Q + cR*R (+ cR0*R0), with
@@ -115,7 +118,8 @@ struct Launch {
   int threads;
 };
 
-template <int N> void launch_e1(const SolveDev& s, const Launch& L, cudaStream_t st);
+// plot != 0: also record the variable-6 sensor (Se6) when AV is on
+template <int N> void launch_e1(const SolveDev& s, const Launch& L, cudaStream_t st, int plot);
 template <int N> void launch_f1(const SolveDev& s, cudaStream_t st);
 template <int N> void launch_e2(const SolveDev& s, const Launch& L, cudaStream_t st);
 template <int N> void launch_f2(const SolveDev& s, cudaStream_t st);
@@ -132,6 +136,12 @@ void launch_point_rusanov(int n, double gam, const double* Qfl, const double* Qf
 void launch_point_iflux(int n, double gam, const double* Qi, double* Fi, double* Gi, cudaStream_t st);
 void launch_point_vflux(int n, double gam, double mu, double eta0, const double* Qv, const double* nQ, double* Fv,
                         double* Gv, cudaStream_t st);
+struct PointAxes {  // flux-point coordinates Xf(1..N+1) of a bound solve, by value
+  double Xf[kMaxN + 1];
+};
+void launch_point_vflux_av(int n, double gam, const PointAxes& ax, const double* muf, const int* fam, const int* ifp,
+                           const int* jfp, const int* ic, const double* Qv, const double* nQ, double* Fv, double* Gv,
+                           cudaStream_t st);
 void launch_reduce_diag(const double* diag, int NC, double* out2, cudaStream_t st);
 
 }  // namespace chorus

@@ -264,6 +264,35 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
       }
     }
   }
+  if (!(sensor & 2)) return;
+  // the same sensor of variable 6 (B_x), whose muAV(6) only the plot output reads
+  // (tecplotter.f90:39 from AV.f90:60-73); in the reference's division form, so a zero
+  // B_x gives the reference's inf or NaN
+  __syncthreads();
+  for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
+    const int e = t / NS, p = t - e * NS, is = p % N, n = p / N;
+    const double* q = sQ + e * NS * 9 + 5;
+    double a = 0.0;
+#pragma unroll
+    for (int m = 0; m < N; m++) a += sA[is * N + m] * q[(n * N + m) * 9];
+    sT[e * NS + p] = a;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
+    const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
+    double a = 0.0;
+#pragma unroll
+    for (int n = 0; n < N; n++) a += sA[js * N + n] * sT[e * NS + n * N + is];
+    const double b = sQ[(e * NS + p) * 9 + 5];
+    sU[e * NS + p] = ((a - b) * (a - b)) / (b * b);
+  }
+  __syncthreads();
+  for (int e = warp; e < cnt; e += nwarp) {
+    double acc = 0.0;
+    for (int p = lane; p < NS; p += 32) acc += sU[e * NS + p];
+    acc = warp_sum(acc);
+    if (lane == 0) s.Se6[e0 + e] = acc;
+  }
 }
 
 template <int N>
@@ -338,13 +367,16 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
 #pragma unroll
       for (int k = 0; k < 9; k++) qr[k] = ql[k];
     }
-    double Fh[8], vnl, ev;
-    rusanov_core(ql, qr, fn.ux, fn.uy, s.gam, fn.msl, Fh, vnl, ev);
+    double vnl, ev;
+    double* fl = s.Fc + gl * 8;
+    double* fr = s.Fc + gr * 8;
+    const double ss = fn.ss;
+    rusanov_emit(ql, qr, fn.ux, fn.uy, s.gam, fn.msl, vnl, ev, [&](int k, double h) {
+      fl[k] = h;
+      if (two) fr[k] = times_sign(h, ss);
+    });
     evb = ev_bits(ev, s.err);
     const double az = vnl > 0.0 ? ql[8] : qr[8];
-    double* fl = s.Fc + gl * 8;
-#pragma unroll
-    for (int k = 0; k < 8; k++) fl[k] = Fh[k];
     s.Azf[gl] = az;
     if (two && s.skip && nfp == 0) {
       const int4 fc = s.face2[f];
@@ -354,9 +386,6 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
       }
     }
     if (two) {
-      double* fr = s.Fc + gr * 8;
-#pragma unroll
-      for (int k = 0; k < 8; k++) fr[k] = times_sign(Fh[k], fn.ss);
       s.Azf[gr] = az;
       double* al = s.Qvf + gl * 9;
       double* ar = s.Qvf + gr * 9;
@@ -381,31 +410,26 @@ __global__ void __launch_bounds__(256) k_f1(SolveDev s) {
 // E2: gradients at solution points and their values at every flux point
 // ---------------------------------------------------------------------------
 template <int N, class O>
-__device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int epb, double* sm) {
+__device__ __forceinline__ void e2_cells(const SolveDev& s, const int* cells, int n, double* sm) {
+  // gradients of the n (<= epb) listed cells; grad A_z (nablaAsp) is computed with the
+  // divergence in the last pass
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
-  __shared__ int list[64];
-
-  double* sQ = sm;                  // [epb][NFP][9]
-  double* sG = sQ + epb * NFP * 9;  // [epb][NS][16]  (d*8 + k)
-  double* sL = sG + epb * NS * 16;  // Lmat (N+1, N)
-  // grad A_z (nablaAsp) is computed with the divergence in the last pass; this pass
-  // only serves the cells whose gradients the viscous fluxes need
-  const int nact = active_cells(s, e0, cnt, 0, list);
-  if (nact == 0) return;
+  double* sQ = sm;                // [n][NFP][9]
+  double* sG = sQ + n * NFP * 9;  // [n][NS][16]  (d*8 + k)
+  double* sL = sG + n * NS * 16;  // Lmat (N+1, N)
   {
     for (int i = threadIdx.x; i < (N + 1) * N; i += blockDim.x) sL[i] = O::ops().L[i];
-    // flux-point states only for the cells whose gradients are needed
-    for (int i = threadIdx.x; i < nact * NFP * 9; i += blockDim.x) {
-      const int le = i / (NFP * 9), r = i - le * (NFP * 9), e = list[le];
-      sQ[e * NFP * 9 + r] = s.Qvf[((size_t)(e0 + e) * NFP) * 9 + r];
+    for (int i = threadIdx.x; i < n * NFP * 9; i += blockDim.x) {
+      const int le = i / (NFP * 9), r = i - le * (NFP * 9);
+      sQ[i] = s.Qvf[(size_t)cells[le] * NFP * 9 + r];
     }
   }
   __syncthreads();
-  // grad Q (variables 1-8) where needed (nablaQsp)
-  for (int t = threadIdx.x; t < nact * NS; t += blockDim.x) {
-    const int le = t / NS, p = t - le * NS, e = list[le], is = p % N, js = p / N;
-    const size_t gs = (size_t)(e0 + e) * NS + p;
-    const double* w = s.gco + (size_t)(e0 + e) * NG * NS + p;
+  // grad Q (variables 1-8) at the solution points (nablaQsp)
+  for (int t = threadIdx.x; t < n * NS; t += blockDim.x) {
+    const int le = t / NS, p = t - le * NS, c = cells[le], is = p % N, js = p / N;
+    const size_t gs = (size_t)c * NS + p;
+    const double* w = s.gco + (size_t)c * NG * NS + p;
     double cx1[N + 1], cx2[N + 1], cy1[N + 1], cy2[N + 1];
 #pragma unroll
     for (int r = 0; r <= N; r++) {
@@ -414,7 +438,7 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
       cy1[r] = w[(2 * (N + 1) + r) * NS];
       cy2[r] = w[(3 * (N + 1) + r) * NS];
     }
-    const double* q = sQ + e * NFP * 9;
+    const double* q = sQ + le * NFP * 9;
     double* out = s.nQs + gs * 18;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -430,15 +454,15 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
       }
       out[k] = gx;
       out[9 + k] = gy;
-      sG[(e * NS + p) * 16 + k] = gx;
-      sG[(e * NS + p) * 16 + 8 + k] = gy;
+      sG[(le * NS + p) * 16 + k] = gx;
+      sG[(le * NS + p) * 16 + 8 + k] = gy;
     }
   }
   __syncthreads();
-  // grad Q at every flux point where needed (nablaQ_interior_FP + face traces)
-  for (int t = threadIdx.x; t < nact * NFP; t += blockDim.x) {
-    const int le = t / NFP, fp = t - le * NFP, e = list[le];
-    const double* G = sG + e * NS * 16;
+  // grad Q at every flux point (nablaQ_interior_FP + face traces)
+  for (int t = threadIdx.x; t < n * NFP; t += blockDim.x) {
+    const int le = t / NFP, fp = t - le * NFP;
+    const double* G = sG + le * NS * 16;
     double acc[16];
 #pragma unroll
     for (int c = 0; c < 16; c++) acc[c] = 0.0;
@@ -459,7 +483,7 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
         for (int c = 0; c < 16; c++) acc[c] += G[(sp * N + ifp) * 16 + c] * l;
       }
     }
-    double* o = s.nQvf + ((size_t)(e0 + e) * NFP + fp) * 18;
+    double* o = s.nQvf + ((size_t)cells[le] * NFP + fp) * 18;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
       o[k] = acc[k];
@@ -468,15 +492,52 @@ __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int 
   }
 }
 
-template <int N>
-__global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb) {
-  extern __shared__ double sm[];
-  const int e0 = blockIdx.x * epb;
-  const int cnt = min(epb, s.NC - e0);
-  if (cnt <= 0) return;
-  e2_body<N, OpsTU>(s, e0, cnt, epb, sm);
+// tile form (batched kernels): the cells of [e0, e0+cnt) whose gradients are needed
+template <int N, class O>
+__device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int epb, double* sm) {
+  __shared__ int list[64];
+  const int nact = active_cells(s, e0, cnt, 0, list);
+  if (nact == 0) return;
+  for (int i = threadIdx.x; i < nact; i += blockDim.x) list[i] += e0;
+  __syncthreads();
+  e2_cells<N, O>(s, list, nact, sm);
 }
 
+// does cell c need its gradients (itself or a face neighbour has viscous work)?
+__device__ __forceinline__ bool needs_gradients(const SolveDev& s, int c) {
+  if (!s.skip || s.nv[c]) return true;
+  const int4 b = s.nbr[c];
+  return (b.x >= 0 && s.nv[b.x]) || (b.y >= 0 && s.nv[b.y]) || (b.z >= 0 && s.nv[b.z]) || (b.w >= 0 && s.nv[b.w]);
+}
+
+// E2 over a chunk of `chunk` (<= blockDim.x) cells per CTA: every thread tests one
+// cell, the CTA compacts the cells that need gradients into an ordered list and runs
+// them in groups of epb, so chunks without viscous work cost one coalesced test
+template <int N>
+__global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb, int chunk) {
+  extern __shared__ double sm[];
+  __shared__ int list[256];
+  __shared__ int woff[9];
+  const int c0 = blockIdx.x * chunk;
+  const int c = c0 + threadIdx.x;
+  const bool need = (int)threadIdx.x < chunk && c < s.NC && needs_gradients(s, c);
+  const unsigned m = __ballot_sync(0xffffffffu, need);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) woff[w + 1] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    woff[0] = 0;
+    for (int i = 1; i <= (int)(blockDim.x >> 5); i++) woff[i] += woff[i - 1];
+  }
+  __syncthreads();
+  if (need) list[woff[w] + __popc(m & ((1u << lane) - 1u))] = c;
+  const int n = woff[blockDim.x >> 5];
+  __syncthreads();
+  for (int g = 0; g < n; g += epb) {
+    e2_cells<N, OpsTU>(s, list + g, min(epb, n - g), sm);
+    __syncthreads();
+  }
+}
 // ---------------------------------------------------------------------------
 // F2: face-averaged gradients and face AV viscosity
 // ---------------------------------------------------------------------------
@@ -532,8 +593,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
 
   double* sF = sm;                  // [epb][NFP][8] total flux Fv - F
   double* sD = sF + epb * NFP * 8;  // [epb][NS] diagnostic partial sums
-  double* sQ = sD + epb * NS;       // [epb][NS][9] state of the block's cells
-  double* sR = sQ + epb * NS * 9;   // [epb][NS][9] residual
+  double* sR = sD + epb * NS;       // [epb][NS][9] residual
   double* sJ = sR + epb * NS * 9;   // [epb][NS] 1/J
   double* sZ = sJ + epb * NS;       // [epb][NFP][2] A_z * (S_x, S_y) at the flux points
   double* sN = sZ + epb * NFP * 2;  // [epb][NS][2] grad A_z
@@ -541,12 +601,11 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
   __shared__ int list[64];
   const int nact = active_cells(s, e0, cnt, 1, list);
   {
-    // every global access of the pass is a contiguous block copy (coalesced), issued
-    // together so their latencies overlap
+    // contiguous block copies (coalesced), issued together so their latencies overlap;
+    // the state itself is read where it is used (the update is elementwise over the
+    // block's contiguous state)
     const double* fi = s.Fc + (size_t)e0 * NFP * 8;
     for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) sF[i] = -fi[i];
-    const size_t q0 = (size_t)e0 * NS * 9;
-    for (int i = threadIdx.x; i < cnt * NS * 9; i += blockDim.x) sQ[i] = s.Q[q0 + i];
     for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sJ[i] = s.invJ[(size_t)e0 * NS + i];
     for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
       const size_t g = (size_t)e0 * NFP + i;
@@ -625,7 +684,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
   __syncthreads();
   // A_z advection (resid(9), compresid.f90:45-47) at every solution point
   for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
-    const double* q = sQ + t * 9;
+    const double* q = s.Q + ((size_t)e0 * NS + t) * 9;
     const double ri = rcp_pos(q[0]);
     const double ax = sN[2 * t] - s.B0y, ay = sN[2 * t + 1] + s.B0x;
     sR[t * 9 + 8] = -(q[1] * ri * ax + q[2] * ri * ay);
@@ -646,12 +705,14 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
     const size_t g0 = (size_t)e0 * NS * 9;
     const int n = cnt * NS * 9;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      const double q = sQ[i], r = sR[i];
       const size_t g = g0 + i;
+      const double q = s.Q[g], r = sR[i];
       if (rk.write_resid) s.resid[g] = r;
       if (!update) continue;
       double qn = rk.cQ * q + rk.cR * r;
-      for (int j = 0; j < rk.nsrc; j++) qn += rk.c[j] * rk.src[j][g];
+#pragma unroll
+      for (int j = 0; j < 3; j++)  // constant indices keep the record in parameter space
+        if (j < rk.nsrc) qn += rk.c[j] * rk.src[j][g];
       if (rk.R0) qn += rk.cR0 * rk.R0[g];
       s.Q[g] = qn;
       if (rk.save_old) rk.save_old[g] = q;

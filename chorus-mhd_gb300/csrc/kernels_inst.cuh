@@ -19,7 +19,7 @@ inline size_t smem_e2(int epb) {
   return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 9 + D<kN>::NS * 16) + (kN + 1) * kN);
 }
 inline size_t smem_e3(int epb) {
-  return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 8 + D<kN>::NS * (1 + 9 + 9 + 1 + 2) + D<kN>::NFP * 2) + (kN + 1) * kN);
+  return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 8 + D<kN>::NS * (1 + 9 + 1 + 2) + D<kN>::NFP * 2) + (kN + 1) * kN);
 }
 inline size_t smem_ct(int epb) { return sizeof(double) * epb * D<kN>::NFP; }
 inline int grid_cells(int nc, int epb) { return (nc + epb - 1) / epb; }
@@ -44,8 +44,9 @@ void CHORUS_CAT(upload_ops_n, CHORUS_N)(const OpsN& o) {
 }
 
 template <>
-void launch_e1<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
-  k_e1<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, s.artiv);
+void launch_e1<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int plot) {
+  const int sensor = s.artiv ? (plot ? 3 : 1) : 0;
+  k_e1<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, sensor);
 }
 void CHORUS_CAT(launch_e1_nosensor_n, CHORUS_N)(const SolveDev& s, const Launch& L, cudaStream_t st) {
   k_e1<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, 0);
@@ -57,7 +58,18 @@ void launch_f1<kN>(const SolveDev& s, cudaStream_t st) {
 }
 template <>
 void launch_e2<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
-  k_e2<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e2(L.epb), st>>>(s, L.epb);
+  // chunks of up to one cell per thread, but small enough for about 16 CTAs per SM
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 152;
+  }
+  int chunk = s.NC / (16 * nsm);
+  chunk = chunk < L.epb ? L.epb : (chunk > L.threads ? L.threads : chunk);
+  chunk -= chunk % L.epb;
+  if (!s.skip) chunk = L.epb;  // every cell needs its gradients: one group per CTA
+  k_e2<kN><<<grid_cells(s.NC, chunk), L.threads, smem_e2(L.epb), st>>>(s, L.epb, chunk);
 }
 template <>
 void launch_f2<kN>(const SolveDev& s, cudaStream_t st) {

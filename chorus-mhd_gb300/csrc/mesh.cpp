@@ -165,6 +165,8 @@ int mesh_load(const std::string& dir, Mesh& m, std::string& err) {
   m.params.DXCYCL = fortran_real(L[19]);
   m.params.DYCYCL = fortran_real(L[20]);
   m.params.ARTIV = std::atoi(L[22].c_str());
+  m.nre = std::atoi(L[24].c_str());
+  m.nwrite = std::atoi(L[25].c_str());
   m.restart = std::atoi(L[27].c_str());
   m.params.gam = 5.0 / 3;
   m.problem = 0;

@@ -147,6 +147,14 @@ int getifluxvectors_gpu(int32_t n, double gam, const double* Qi /*n x 8*/, doubl
 int getvfluxvectors_gpu(int32_t n, double gam, double mu, double eta0, const double* Qv /*n x 9*/,
                         const double* nablaQ /*n x 18, (9,2) per point*/, double* Fv /*n x 9*/,
                         double* Gv /*n x 9*/);
+/* getVfluxvectors_AV(Qv,nablaQ,Fv,Gv,fam,ifp,jfp,ic) (getrusanov.f90:251-360) over n
+ * points of a bound solve: mu_art interpolated at flux point (ifp,jfp) of family fam
+ * (1 or 2) of cell ic, all 1-based as in the reference, from the face AV viscosities
+ * muAVfi/muAVfj that the context's last residual evaluation left (:273-281);
+ * eta_art = 0.  Out-of-range indices return CHORUS_EINVAL before any device work. */
+int getvfluxvectors_av_gpu(ChorusCtx* ctx, int32_t n, const double* Qv /*n x 9*/,
+                           const double* nablaQ /*n x 18*/, double* Fv /*n x 9*/, double* Gv /*n x 9*/,
+                           const int32_t* fam, const int32_t* ifp, const int32_t* jfp, const int32_t* ic);
 /* getrusanovflux_gpu for callers that cannot allocate device memory (no counterpart in
  * the reference): a host whose device memory is all held by its own pool, or one with
  * work in flight that a cudaFree would stall.  Same arguments and results; the device
@@ -267,6 +275,41 @@ int chorus_initial_state(const ChorusMesh* mesh, ChorusCtx* ctx, double* Q);
  * float64 ctime, then per cell int32 global id + Q(9,N,N). */
 int chorus_write_restart(ChorusCtx* ctx, const char* path, int32_t iter, double ctime);
 int chorus_read_restart(ChorusCtx* ctx, const char* path, int32_t* iter, double* ctime);
+
+/* ------------------------------------------------------------------------------
+ * Plot output (iterations.f90:80-84 for one partition): tecplotter2dsetup
+ * (tecplotter2dsetup.f90:1-177) on the host at create, tecplotter2d
+ * (tecplotter.f90:1-86) on the device at every evaluation, tecpost_parallel
+ * (tecplotter.f90:92-418) as a headless file write.  The node values use the Q of the
+ * bound solve and the muAV(1), muAV(6) of its last stage (the sensor of variable 6 is
+ * recorded in the last stage of every step and by compresid_gpu).  With ARTIV = 0 the
+ * reference never allocates muAV; the muAV/etaAV fields are zeros here.
+ * --------------------------------------------------------------------------- */
+typedef struct ChorusPlot ChorusPlot;
+/* IVCELL(NCELL,4), IC2F(NCELL,4) 1-based, XV/YV(NVERT), Xs(N) as in the reference;
+ * NRE sub-intervals per cell edge (readinput.f90:32). */
+int chorus_plot_create(ChorusCtx* ctx, const int32_t* IVCELL, const int32_t* IC2F, const double* XV,
+                       const double* YV, int32_t NVERT, int32_t NFACE, const double* Xs, int32_t NRE,
+                       ChorusPlot** plot);
+/* the same from a loaded case; NRE <= 0 takes the case file's NRE */
+int chorus_plot_create_mesh(ChorusCtx* ctx, const ChorusMesh* mesh, int32_t NRE, ChorusPlot** plot);
+int chorus_plot_free(ChorusPlot* plot);
+/* plotnodes, plotcells; warned = 1 where the reference prints its 'something wrong'
+ * checks (tecplotter2dsetup.f90:54-56, :99-106) */
+int chorus_plot_info(const ChorusPlot* plot, int64_t* nodes, int64_t* cells, int32_t* warned);
+/* evaluate on the device and copy out (any pointer may be NULL): plotX(2,nodes),
+ * plotQ(9,nodes) = rho u v w p Bx By Bz Az, plotAV(2,nodes) = muAV etaAV,
+ * connec(4,cells) 1-based, gnode_factor(nodes) */
+int chorus_plot_values(ChorusPlot* plot, double* plotX, double* plotQ, double* plotAV, int32_t* connec,
+                       int32_t* gnode_factor);
+/* 'TEC' // i7.7 int(ctime) // the f6.3 fraction without its integer digit // '.plt' */
+int chorus_plot_filename(double ctime, char* buf, int32_t n);
+/* evaluate and write dir/<chorus_plot_filename(ctime)>: #!TDV111, one
+ * FEQUADRILATERAL zone, 13 float32 variables in block packing, 0-based connectivity;
+ * the written path goes to path_out when given */
+int chorus_plot_write(ChorusPlot* plot, double ctime, const char* dir, char* path_out, int32_t path_len);
+/* NRE and nwrite of a loaded case (readinput.f90:32-33) */
+int chorus_mesh_output_info(const ChorusMesh* mesh, int32_t* nre, int32_t* nwrite);
 
 #ifdef __cplusplus
 }

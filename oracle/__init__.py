@@ -72,6 +72,10 @@ def lib():
         L.orc_getrusanovflux.argtypes = [ctypes.c_double, dp, dp, dp, dp, dp, dp, ip, ip, dp, dp]
         L.orc_getifluxvectors.argtypes = [ctypes.c_double, dp, dp, dp]
         L.orc_getvfluxvectors.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp, dp, dp]
+        L.orc_plot_setup.argtypes = [vp, ip]
+        L.orc_plot_eval.argtypes = [vp]
+        L.orc_plot_filename.argtypes = [ctypes.c_double, cp, ip]
+        L.orc_plot_write.argtypes = [vp, ctypes.c_double, cp]
         _lib = L
     return _lib
 
@@ -126,6 +130,18 @@ class Oracle:
 
     def compresid(self):
         self.L.orc_compresid(self._h)
+
+    def plot_setup(self, nre: int) -> int:
+        """tecplotter2dsetup; returns 1 where the reference would print its warnings."""
+        return self.L.orc_plot_setup(self._h, int(nre))
+
+    def plot_eval(self):
+        if self.L.orc_plot_eval(self._h) != 0:
+            raise RuntimeError("plot_setup first")
+
+    def plot_write(self, ctime: float, path: str):
+        if self.L.orc_plot_write(self._h, float(ctime), path.encode()) != 0:
+            raise RuntimeError("cannot write " + path)
 
     def compflux(self):
         self.L.orc_compflux(self._h)
@@ -194,3 +210,10 @@ def getvfluxvectors(gam, mu, eta0, Qv, nablaQ):
     Gv = np.zeros(9)
     L.orc_getvfluxvectors(gam, mu, eta0, _dp(Qv), _dp(nq), _dp(Fv), _dp(Gv))
     return Fv, Gv
+
+
+def plot_filename(ctime: float) -> str:
+    """The reference's plot file name for solution time ctime (tecplotter.f90:179-180)."""
+    b = ctypes.create_string_buffer(64)
+    lib().orc_plot_filename(float(ctime), b, 64)
+    return b.value.decode()

@@ -64,6 +64,10 @@ struct orc {
   double *Qk0, *Qka, *qj2, *qj3, *resid0;
   double ctime, eigvmax, eigvmax_g, epsilon0;
   int iter;
+  /* plot output (tecplotter2dsetup.f90, tecplotter.f90) */
+  int plot_nre, plotnodes, plotcells;
+  int *gnumnode, *gnode_factor, *connec_c2n;
+  double *plotX, *plotQ, *plotAV;
 };
 
 /* ---------- index helpers (0-based, Fortran column-major) ---------- */
@@ -1655,9 +1659,263 @@ void orc_free(orc_t* o) {
                   o->Xs, o->Xf, o->Lmat, o->Mmat, o->Xs_low, o->Xf_low, o->dmdxs, o->dmdxf1, o->dmdxf2,
                   o->Jac, o->S1, o->S2, o->XXsolu, o->Q, o->F1, o->G2, o->Fv1, o->Gv2, o->resid, o->Qvfi,
                   o->Qvfj, o->nablaQs, o->nablaQvfi, o->nablaQvfj, o->Azfi, o->Azfj, o->nablaAs, o->muAV,
-                  o->muAVfi, o->muAVfj, o->SM_IND, o->Qk0, o->Qka, o->qj2, o->qj3, o->resid0};
+                  o->muAVfi, o->muAVfj, o->SM_IND, o->Qk0, o->Qka, o->qj2, o->qj3, o->resid0,
+                  o->gnumnode, o->gnode_factor, o->connec_c2n, o->plotX, o->plotQ, o->plotAV};
   for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++) free(ptrs[i]);
   free(o);
+}
+
+/* =====================================================================
+ * Plot output for one rank: tecplotter2dsetup (tecplotter2dsetup.f90:1-177),
+ * tecplotter2d (tecplotter.f90:1-86), tecpost_parallel (tecplotter.f90:92-418).
+ * smooth_procint_plot (smooth_procint_plot.f90) only adds the contributions of nodes
+ * on processor interfaces; with one partition there are none.
+ * ===================================================================== */
+/* distcalc tecplotter2dsetup.f90:160-172 */
+static double plot_dist(const orc_t* o, const double xx[2], int gnid) {
+  double d = sqrt((xx[0] - o->plotX[2 * (gnid - 1)]) * (xx[0] - o->plotX[2 * (gnid - 1)]) +
+                  (xx[1] - o->plotX[2 * (gnid - 1) + 1]) * (xx[1] - o->plotX[2 * (gnid - 1) + 1]));
+  return fabs(d);
+}
+
+/* tecplotter2dsetup.f90:1-177 (CURVE_WALL = 0); gnumnode(ii,jj,icell) 1-based values */
+int orc_plot_setup(orc_t* o, int nre) {
+  const int Np = nre, NC = o->NCELL;
+  if (Np < 1) return -1;
+  free(o->gnumnode); free(o->gnode_factor); free(o->connec_c2n); free(o->plotX);
+  free(o->plotQ); free(o->plotAV);
+  o->plotQ = o->plotAV = NULL;
+  const int64_t nn = (int64_t)(Np + 1) * (Np + 1) * NC;
+  o->gnumnode = ialloc(nn);
+  o->gnode_factor = ialloc(nn);
+  o->plotX = dalloc(2 * nn);
+  o->connec_c2n = ialloc(4 * (int64_t)Np * Np * NC);
+  int* isfacenod = ialloc(o->NFACE);
+  const int ne = Np - 1 > 0 ? Np - 1 : 1;
+  int* gfacenode = ialloc((int64_t)ne * o->NFACE);
+  int plotnodes = 0, plotcells = 0, bad = 0;
+  const double tolplot = 1e-5;
+#define GNUM(ii, jj, ic) o->gnumnode[((ii) - 1) + (Np + 1) * (((jj) - 1) + (Np + 1) * (int64_t)(ic))]
+  /* the 4 vertices of each cell are global nodes :30-52 */
+  for (int ic = 0; ic < NC; ic++) {
+    int v[4];
+    for (int k = 0; k < 4; k++) v[k] = IVCELL_(o, ic, k);
+    GNUM(1, 1, ic) = v[0];
+    GNUM(Np + 1, 1, ic) = v[1];
+    GNUM(Np + 1, Np + 1, ic) = v[2];
+    GNUM(1, Np + 1, ic) = v[3];
+    for (int k = 0; k < 4; k++) {
+      int gnid = v[k];
+      if (o->gnode_factor[gnid - 1] == 0) {
+        plotnodes++;
+        o->plotX[2 * (gnid - 1)] = o->XV[gnid - 1];
+        o->plotX[2 * (gnid - 1) + 1] = o->YV[gnid - 1];
+      }
+      o->gnode_factor[gnid - 1]++;
+    }
+  }
+  if (plotnodes != o->NVERT) bad = 1; /* :54-56 */
+  for (int ic = 0; ic < NC; ic++) {
+    double xs[2][4];
+    for (int j = 0; j < 4; j++) {
+      xs[0][j] = o->XV[IVCELL_(o, ic, j) - 1];
+      xs[1][j] = o->YV[IVCELL_(o, ic, j) - 1];
+    }
+    /* nodes on the 4 faces, shared with the neighbour through the face :67-123 */
+    for (int k = 1; k <= 4; k++) {
+      int iface = IC2F_(o, ic, k - 1);
+      for (int enode = 1; enode <= Np - 1; enode++) {
+        int ii, jj;
+        switch (k) {
+          case 1: ii = enode + 1; jj = 1; break;
+          case 2: ii = Np + 1; jj = enode + 1; break;
+          case 3: ii = Np + 1 - enode; jj = Np + 1; break;
+          default: ii = 1; jj = Np + 1 - enode; break;
+        }
+        double xsi = (double)(ii - 1) / (double)Np, eta = (double)(jj - 1) / (double)Np, rx[2];
+        xycoor(xs, xsi, eta, rx);
+        if (isfacenod[iface - 1] == 1) {
+          int checkmatch = 0;
+          for (int existnode = 1; existnode <= Np - 1; existnode++) {
+            int gnid = gfacenode[(existnode - 1) + (int64_t)ne * (iface - 1)];
+            if (plot_dist(o, rx, gnid) <= tolplot) {
+              GNUM(ii, jj, ic) = gnid;
+              o->gnode_factor[gnid - 1]++;
+              checkmatch = 1;
+            }
+          }
+          if (!checkmatch) bad = 1;
+        } else {
+          plotnodes++;
+          o->plotX[2 * (plotnodes - 1)] = rx[0];
+          o->plotX[2 * (plotnodes - 1) + 1] = rx[1];
+          GNUM(ii, jj, ic) = plotnodes;
+          gfacenode[(enode - 1) + (int64_t)ne * (iface - 1)] = plotnodes;
+          o->gnode_factor[plotnodes - 1]++;
+        }
+      }
+      if (isfacenod[iface - 1] == 0) isfacenod[iface - 1] = 1;
+    }
+    /* interior nodes :127-137 */
+    for (int ii = 2; ii <= Np; ii++)
+      for (int jj = 2; jj <= Np; jj++) {
+        double xsi = (double)(ii - 1) / (double)Np, eta = (double)(jj - 1) / (double)Np, rx[2];
+        xycoor(xs, xsi, eta, rx);
+        plotnodes++;
+        o->plotX[2 * (plotnodes - 1)] = rx[0];
+        o->plotX[2 * (plotnodes - 1) + 1] = rx[1];
+        GNUM(ii, jj, ic) = plotnodes;
+        o->gnode_factor[plotnodes - 1]++;
+      }
+    /* plot cells :139-148 */
+    for (int ii = 1; ii <= Np; ii++)
+      for (int jj = 1; jj <= Np; jj++) {
+        plotcells++;
+        int* c = o->connec_c2n + 4 * (int64_t)(plotcells - 1);
+        c[0] = GNUM(ii, jj, ic);
+        c[1] = GNUM(ii + 1, jj, ic);
+        c[2] = GNUM(ii + 1, jj + 1, ic);
+        c[3] = GNUM(ii, jj + 1, ic);
+      }
+  }
+#undef GNUM
+  free(isfacenod);
+  free(gfacenode);
+  o->plot_nre = Np;
+  o->plotnodes = plotnodes;
+  o->plotcells = plotcells;
+  return bad ? 1 : 0;
+}
+
+/* hval tecplotter.f90:62-82: Lagrange basis i (1-based) through Xs at xval */
+static double plot_hval(const orc_t* o, int np, int i, double xval) {
+  double hvaln = 1.0, hvald = 1.0;
+  for (int s = 1; s <= np; s++)
+    if (s != i) {
+      hvaln = hvaln * (xval - o->Xs[s - 1]);
+      hvald = hvald * (o->Xs[i - 1] - o->Xs[s - 1]);
+    }
+  return hvaln / hvald;
+}
+
+/* tecplotter2d tecplotter.f90:1-59: conservative state summed over the cells sharing a
+ * node, averaged, converted to (rho,u,v,w,p,Bx,By,Bz,Az); muAV(1) and muAV(6) likewise.
+ * With ARTIV = 0 the reference never allocates muAV; the plot carries zeros there. */
+int orc_plot_eval(orc_t* o) {
+  if (!o->gnumnode) return -1;
+  const int Np = o->plot_nre, N = o->N;
+  free(o->plotQ); free(o->plotAV);
+  o->plotQ = dalloc(9 * (int64_t)o->plotnodes);
+  o->plotAV = dalloc(2 * (int64_t)o->plotnodes);
+  for (int ic = 0; ic < o->NCELL; ic++)
+    for (int jj = 1; jj <= Np + 1; jj++)
+      for (int ii = 1; ii <= Np + 1; ii++) {
+        double xsi = (double)(ii - 1) / (double)Np, eta = (double)(jj - 1) / (double)Np;
+        int gnid = o->gnumnode[(ii - 1) + (Np + 1) * ((jj - 1) + (Np + 1) * (int64_t)ic)];
+        double Qs[NV] = {0};
+        for (int js = 1; js <= N; js++)
+          for (int is = 1; is <= N; is++)
+            for (int k = 0; k < NV; k++)
+              Qs[k] = Qs[k] + o->Q[IDX_Q(o, k, is - 1, js - 1, ic)] * plot_hval(o, N, is, xsi) * plot_hval(o, N, js, eta);
+        for (int k = 0; k < NV; k++) o->plotQ[k + 9 * (int64_t)(gnid - 1)] += Qs[k];
+        if (o->ARTIV == 1) {
+          o->plotAV[2 * (int64_t)(gnid - 1)] += o->muAV[0 + 9 * ic];
+          o->plotAV[2 * (int64_t)(gnid - 1) + 1] += o->muAV[5 + 9 * ic];
+        }
+      }
+  const double gam = o->gam;
+  for (int nd = 0; nd < o->plotnodes; nd++) {
+    double* pq = o->plotQ + 9 * (int64_t)nd;
+    double Qs[NV];
+    for (int k = 0; k < NV; k++) Qs[k] = pq[k] / (double)o->gnode_factor[nd];
+    pq[0] = Qs[0];
+    pq[1] = Qs[1] / Qs[0];
+    pq[2] = Qs[2] / Qs[0];
+    pq[3] = Qs[3] / Qs[0];
+    for (int k = 5; k < 9; k++) pq[k] = Qs[k];
+    double NORM_U = pq[1] * pq[1] + pq[2] * pq[2] + pq[3] * pq[3];
+    double NORM_B = pq[5] * pq[5] + pq[6] * pq[6] + pq[7] * pq[7];
+    pq[4] = (Qs[4] - 0.5 * Qs[0] * NORM_U - 0.5 * NORM_B) * (gam - 1);
+    o->plotAV[2 * (int64_t)nd] = o->plotAV[2 * (int64_t)nd] / (double)o->gnode_factor[nd];
+    o->plotAV[2 * (int64_t)nd + 1] = o->plotAV[2 * (int64_t)nd + 1] / (double)o->gnode_factor[nd];
+  }
+  return 0;
+}
+
+/* write_tecplot_string tecplotter.f90:399-416: characters as int32, then a zero */
+static void tec_string(FILE* f, const char* s) {
+  int32_t v;
+  for (; *s; s++) { v = (unsigned char)*s; fwrite(&v, 4, 1, f); }
+  v = 0;
+  fwrite(&v, 4, 1, f);
+}
+
+/* file name tecplotter.f90:179-180: 'TEC', int(ctime) as i7.7, the fraction written
+ * with f6.3 minus its leading blank and integer digit, '.plt' */
+int orc_plot_filename(double ctime, char* out, int n) {
+  char dec[32];
+  snprintf(dec, sizeof dec, "%6.3f", ctime - (double)(int)ctime);
+  return snprintf(out, (size_t)n, "TEC%07d%.4s.plt", (int)ctime, dec + 2);
+}
+
+/* tecpost_parallel tecplotter.f90:92-418 for one rank: Tecplot binary (#!TDV111), one
+ * FEQUADRILATERAL zone, block packing, float32 fields, 0-based connectivity */
+int orc_plot_write(const orc_t* o, double ctime, const char* path) {
+  if (!o->plotQ) return -1;
+  FILE* f = fopen(path, "wb");
+  if (!f) return -1;
+  const int nvar = 13, n = o->plotnodes;
+  double minmax[2 * 13];
+  for (int v = 0; v < nvar; v++) {
+    double lo = 0, hi = 0;
+    for (int nd = 0; nd < n; nd++) {
+      double x = v < 2 ? o->plotX[2 * (int64_t)nd + v] : v < 11 ? o->plotQ[9 * (int64_t)nd + (v - 2)]
+                                                                 : o->plotAV[2 * (int64_t)nd + (v - 11)];
+      if (nd == 0 || x < lo) lo = x;
+      if (nd == 0 || x > hi) hi = x;
+    }
+    minmax[2 * v] = lo;
+    minmax[2 * v + 1] = hi;
+  }
+  const float ZONEMARKER = 299.0f, EOHMARKER = 357.0f;
+  fwrite("#!TDV111", 1, 8, f);
+  int32_t it[16] = {1, 0};
+  fwrite(it, 4, 2, f);
+  tec_string(f, "step data");
+  int32_t nv = nvar;
+  fwrite(&nv, 4, 1, f);
+  const char* names[13] = {"X", "Y", "RHO", "U", "V", "W", "P", "Bx", "By", "Bz", "Az", "muAV", "etaAV"};
+  for (int v = 0; v < nvar; v++) tec_string(f, names[v]);
+  fwrite(&ZONEMARKER, 4, 1, f);
+  tec_string(f, "ZONE 001");
+  int32_t pz[2] = {-1, 0};
+  fwrite(pz, 4, 2, f);
+  fwrite(&ctime, 8, 1, f);
+  int32_t zh[12] = {-1, 3, 0, 0, 0, 0, n, o->plotcells, 0, 0, 0, 0};
+  fwrite(zh, 4, 12, f);
+  fwrite(&EOHMARKER, 4, 1, f);
+  fwrite(&ZONEMARKER, 4, 1, f);
+  for (int v = 0; v < nvar; v++) it[v] = 1;
+  it[nvar] = 0;
+  it[nvar + 1] = 0;
+  it[nvar + 2] = -1;
+  fwrite(it, 4, nvar + 3, f);
+  fwrite(minmax, 8, 2 * nvar, f);
+  float* buf = (float*)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+  for (int v = 0; v < nvar; v++) {
+    for (int nd = 0; nd < n; nd++)
+      buf[nd] = (float)(v < 2 ? o->plotX[2 * (int64_t)nd + v] : v < 11 ? o->plotQ[9 * (int64_t)nd + (v - 2)]
+                                                                        : o->plotAV[2 * (int64_t)nd + (v - 11)]);
+    fwrite(buf, 4, (size_t)n, f);
+  }
+  free(buf);
+  for (int64_t i = 0; i < 4 * (int64_t)o->plotcells; i++) {
+    int32_t c = o->connec_c2n[i] - 1;
+    fwrite(&c, 4, 1, f);
+  }
+  int rc = ferror(f) ? -1 : 0;
+  fclose(f);
+  return rc;
 }
 
 /* =====================================================================
@@ -1717,6 +1975,9 @@ int orc_geti(const orc_t* o, const char* n) {
   if (!strcmp(n, "iter")) return o->iter;
   if (!strcmp(n, "problem")) return o->problem;
   if (!strcmp(n, "nwrite")) return o->nwrite;
+  if (!strcmp(n, "NRE")) return o->NRE;
+  if (!strcmp(n, "plotnodes")) return o->plotnodes;
+  if (!strcmp(n, "plotcells")) return o->plotcells;
   return -1;
 }
 double orc_getd(const orc_t* o, const char* n) {
@@ -1764,7 +2025,8 @@ double* orc_darray(orc_t* o, const char* n, int64_t* count) {
       {"Xf", o->Xf, N + 1},          {"XV", o->XV, o->NVERT},          {"YV", o->YV, o->NVERT},
       {"muAV", o->muAV, 9 * NC},     {"muAVfi", o->muAVfi, 18 * NC},   {"muAVfj", o->muAVfj, 18 * NC},
       {"SM_IND", o->SM_IND, 9 * NC}, {"XXsolu", o->XXsolu, 2 * ns},    {"Qk0", o->Qk0, 9 * ns},
-      {"Xs_low", o->Xs_low, N - 1},
+      {"Xs_low", o->Xs_low, N - 1},  {"plotX", o->plotX, 2 * (int64_t)o->plotnodes},
+      {"plotQ", o->plotQ, 9 * (int64_t)o->plotnodes}, {"plotAV", o->plotAV, 2 * (int64_t)o->plotnodes},
   };
   for (size_t i = 0; i < sizeof t / sizeof t[0]; i++)
     if (!strcmp(n, t[i].name)) { if (count) *count = t[i].c; return t[i].p; }
@@ -1780,6 +2042,8 @@ int32_t* orc_iarray(orc_t* o, const char* n, int64_t* count) {
       {"IBFCYC", o->IBFCYC, o->NCYCL},            {"IBFCYCLOC", o->IBFCYCLOC, o->NCYCLOC},
       {"CYC2FPAIR", o->CYC2FPAIR, 2 * (int64_t)o->NPAIR},
       {"iface2fp", o->iface2fp, 4 * (int64_t)o->N}, {"jface2fp", o->jface2fp, 4 * (int64_t)o->N},
+      {"gnumnode", o->gnumnode, (int64_t)(o->plot_nre + 1) * (o->plot_nre + 1) * o->NCELL},
+      {"gnode_factor", o->gnode_factor, o->plotnodes}, {"connec_c2n", o->connec_c2n, 4 * (int64_t)o->plotcells},
   };
   for (size_t i = 0; i < sizeof t / sizeof t[0]; i++)
     if (!strcmp(n, t[i].name)) { if (count) *count = t[i].c; return (int32_t*)t[i].p; }

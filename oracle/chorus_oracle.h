@@ -68,6 +68,17 @@ int orc_run(orc_t* o, int nsteps);
 int orc_write_restart(const orc_t* o, const char* path);
 int orc_read_restart(orc_t* o, const char* path);
 
+/* Plot output for one rank (tecplotter2dsetup.f90:1-177, tecplotter.f90:1-418):
+ * plot nodes with NRE sub-intervals per cell edge (0 = ok, 1 = the reference's
+ * 'something wrong' warnings fired), node values from the current Q and muAV, the
+ * reference's file name for ctime, and the Tecplot binary file.  Arrays afterwards:
+ * plotX(2,n) plotQ(9,n) plotAV(2,n), gnumnode(NRE+1,NRE+1,NCELL) gnode_factor(n)
+ * connec_c2n(4,cells) (1-based). */
+int orc_plot_setup(orc_t* o, int nre);
+int orc_plot_eval(orc_t* o);
+int orc_plot_filename(double ctime, char* out, int n);
+int orc_plot_write(const orc_t* o, double ctime, const char* path);
+
 /* Number of OpenMP threads used by cell/face loops (1 when built without OpenMP). */
 int orc_set_threads(int n);
 

@@ -84,3 +84,54 @@ def test_vflux_points(mu, eta0):
         a, b = oracle.getvfluxvectors(gam, mu, eta0, Q[i], G[i])
         assert np.abs(Fv[i] - a).max() <= TOL * (np.abs(a).max() + 1e-300) + 1e-300
         assert np.abs(Gv[i] - b).max() <= TOL * (np.abs(b).max() + 1e-300) + 1e-300
+
+
+def test_vflux_av_points_use_the_solve_face_viscosity(case_root):
+    """getVfluxvectors_AV(Qv,nablaQ,Fv,Gv,fam,ifp,jfp,ic) on a bound solve: mu_art from
+    the face viscosities its last compresid left, against the oracle's own muAVfi/j."""
+    from chorus_mhd import Mesh, Solver
+    from helpers import make_case
+    d = make_case(case_root, problem="rotor", nx=64, ny=64, N=3, jitter=0.1, seed=6)
+    o = oracle.Oracle(d)
+    o.run(2)
+    s = Solver(Mesh(d), initial_state=False)
+    s.upload(o.array("Q").copy())
+    o.compresid()
+    s.compresid()
+    N, NC, gam = s.N, s.ncell, o.getd("gam")
+    Xf = o.array("Xf")
+    mfi = o.array("muAVfi").reshape(NC, 2, 9)[:, :, 0]
+    mfj = o.array("muAVfj").reshape(NC, 2, 9)[:, :, 0]
+    hot = np.flatnonzero((mfi > 0).any(1) | (mfj > 0).any(1))
+    assert hot.size > 0, "the case must have AV somewhere"
+    rng = np.random.default_rng(11)
+    n = 600
+    fam = rng.integers(1, 3, n).astype(np.int32)
+    ifp = np.where(fam == 1, rng.integers(1, N + 2, n), rng.integers(1, N + 1, n)).astype(np.int32)
+    jfp = np.where(fam == 1, rng.integers(1, N + 1, n), rng.integers(1, N + 2, n)).astype(np.int32)
+    ic = np.where(rng.random(n) < 0.7, rng.choice(hot, n) + 1, rng.integers(1, NC + 1, n)).astype(np.int32)
+    Q = random_states(rng, n)
+    G = rng.normal(size=(n, 18))
+    Fv, Gv = np.zeros((n, 9)), np.zeros((n, 9))
+    L = _lib.load()
+    _lib.check(L.getvfluxvectors_av_gpu(s._ctx, n, _dp(Q), _dp(G), _dp(Fv), _dp(Gv), _ip(fam), _ip(ifp), _ip(jfp),
+                                        _ip(ic)))
+    worst = 0.0
+    for i in range(n):
+        c = ic[i] - 1
+        if fam[i] == 1:
+            x = Xf[ifp[i] - 1]
+            mu_art = mfi[c, 0] * (1.0 - x) + mfi[c, 1] * x
+        else:
+            x = Xf[jfp[i] - 1]
+            mu_art = mfj[c, 0] * (1.0 - x) + mfj[c, 1] * x
+        a, b = oracle.getvfluxvectors(gam, mu_art, 0.0, Q[i], G[i])
+        scale = max(1e-300, np.abs(a).max(), np.abs(b).max())
+        worst = max(worst, np.abs(Fv[i] - a).max() / scale, np.abs(Gv[i] - b).max() / scale)
+    assert worst <= 1e-11, worst
+    # indices outside the solve are refused before any device work
+    bad = ic.copy()
+    bad[3] = NC + 1
+    assert L.getvfluxvectors_av_gpu(s._ctx, n, _dp(Q), _dp(G), _dp(Fv), _dp(Gv), _ip(fam), _ip(ifp), _ip(jfp),
+                                    _ip(bad)) == 1
+    s.close()
