@@ -355,8 +355,8 @@ def run_serving(args, device, tmp):
 # per element per RK stage, from ncu on the five stage kernels (Orszag-Tang 192x192,
 # N=5, after the warm-up steps): FP64 thread instructions (DFMA + DADD + DMUL) and flops
 # (2*DFMA + DADD + DMUL); DRAM bytes read + written
-FP64_PER_ELEMENT_STAGE: dict = {}
-TRAFFIC_PER_ELEMENT_STAGE: dict = {}
+FP64_PER_ELEMENT_STAGE: dict = {5: (11044, 17679)}
+TRAFFIC_PER_ELEMENT_STAGE: dict = {5: 26840}
 
 
 def cpu_baseline(case_dir, dof, warm=1, timed=2):

@@ -367,16 +367,13 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
 #pragma unroll
       for (int k = 0; k < 9; k++) qr[k] = ql[k];
     }
-    double vnl, ev;
-    double* fl = s.Fc + gl * 8;
-    double* fr = s.Fc + gr * 8;
-    const double ss = fn.ss;
-    rusanov_emit(ql, qr, fn.ux, fn.uy, s.gam, fn.msl, vnl, ev, [&](int k, double h) {
-      fl[k] = h;
-      if (two) fr[k] = times_sign(h, ss);
-    });
+    double Fh[8], vnl, ev;
+    rusanov_core(ql, qr, fn.ux, fn.uy, s.gam, fn.msl, Fh, vnl, ev);
     evb = ev_bits(ev, s.err);
     const double az = vnl > 0.0 ? ql[8] : qr[8];
+    double* fl = s.Fc + gl * 8;
+#pragma unroll
+    for (int k = 0; k < 8; k++) fl[k] = Fh[k];
     s.Azf[gl] = az;
     if (two && s.skip && nfp == 0) {
       const int4 fc = s.face2[f];
@@ -386,6 +383,9 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
       }
     }
     if (two) {
+      double* fr = s.Fc + gr * 8;
+#pragma unroll
+      for (int k = 0; k < 8; k++) fr[k] = times_sign(Fh[k], fn.ss);
       s.Azf[gr] = az;
       double* al = s.Qvf + gl * 9;
       double* ar = s.Qvf + gr * 9;
@@ -710,9 +710,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
       if (rk.write_resid) s.resid[g] = r;
       if (!update) continue;
       double qn = rk.cQ * q + rk.cR * r;
-#pragma unroll
-      for (int j = 0; j < 3; j++)  // constant indices keep the record in parameter space
-        if (j < rk.nsrc) qn += rk.c[j] * rk.src[j][g];
+      for (int j = 0; j < rk.nsrc; j++) qn += rk.c[j] * rk.src[j][g];
       if (rk.R0) qn += rk.cR0 * rk.R0[g];
       s.Q[g] = qn;
       if (rk.save_old) rk.save_old[g] = q;

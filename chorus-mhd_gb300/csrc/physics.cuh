@@ -74,66 +74,55 @@ __host__ __device__ __forceinline__ void iflux_contra(const double* q, double sx
   F[7] = Bz * Un - w * Bn;
 }
 
-// One side of a face point for the Rusanov flux: velocity, total pressure and normal
-// components (getrusanov.f90:19-75).
-struct RusanovSide {
-  double u, v, w, p, pt, Vn, Bn, uB;
-};
-__host__ __device__ __forceinline__ RusanovSide rusanov_side(const double* q, double ux, double uy, double gm1) {
-  RusanovSide r;
-  const double ri = rcp_pos(q[0]);
-  r.u = ri * q[1];
-  r.v = ri * q[2];
-  r.w = ri * q[3];
-  const double B2 = q[5] * q[5] + q[6] * q[6] + q[7] * q[7];
-  r.p = gm1 * (q[4] - 0.5 * q[0] * (r.u * r.u + r.v * r.v + r.w * r.w) - B2 * 0.5);
-  r.pt = r.p + 0.5 * B2;
-  r.Vn = r.u * ux + r.v * uy;
-  r.Bn = q[5] * ux + q[6] * uy;
-  r.uB = r.u * q[5] + r.v * q[6] + r.w * q[7];
-  return r;
-}
-// component k of the normal ideal-MHD flux of one side
-__host__ __device__ __forceinline__ double rusanov_flux(const double* q, const RusanovSide& r, double ux, double uy,
-                                                        int k) {
-  switch (k) {
-    case 0: return q[0] * r.Vn;
-    case 1: return q[1] * r.Vn + r.pt * ux - q[5] * r.Bn;
-    case 2: return q[2] * r.Vn + r.pt * uy - q[6] * r.Bn;
-    case 3: return q[3] * r.Vn - q[7] * r.Bn;
-    case 4: return (q[4] + r.pt) * r.Vn - r.Bn * r.uB;
-    case 5: return (r.v * q[5] - r.u * q[6]) * uy;
-    case 6: return (r.u * q[6] - r.v * q[5]) * ux;
-    default: return q[7] * r.Vn - r.w * r.Bn;
-  }
-}
-
 // Rusanov flux of getrusanovflux (getrusanov.f90:1-109) along the unit normal (ux,uy),
-// times `scale`: component k is emit(k, scale*(Fl + Fr - eigv*(qr - ql))); with scale =
-// magnorm*sign_l/2 this is the reference's Fnl in the left cell's computational frame
-// (:90-93).  The components are handed out as they are formed, so no flux array stays
-// live.  Returns the left normal velocity (for the A_z upwinding, :99-103) and the
-// wave-speed bound eigv (:87).
-template <class Emit>
-__host__ __device__ __forceinline__ void rusanov_emit(const double* ql, const double* qr, double ux, double uy,
-                                                      double gam, double scale, double& vnl, double& eigv,
-                                                      Emit&& emit) {
+// times `scale`: Fh = scale*(Fl + Fr - eigv*(qr - ql)); with scale = magnorm*sign_l/2
+// this is the reference's Fnl in the left cell's computational frame (:90-93).  Returns
+// the left normal velocity (for the A_z upwinding, :99-103) and the wave-speed bound
+// eigv (:87).
+__host__ __device__ __forceinline__ void rusanov_core(const double* ql, const double* qr, double ux, double uy,
+                                                      double gam, double scale, double* Fh, double& vnl,
+                                                      double& eigv) {
   const double gm1 = gam - 1.0;
-  const RusanovSide L = rusanov_side(ql, ux, uy, gm1), R = rusanov_side(qr, ux, uy, gm1);
+  double Fl[8], Fr[8], pgl, pgr, vn[2];
+  const double* qs[2] = {ql, qr};
+  double* Fs[2] = {Fl, Fr};
+  double* pg[2] = {&pgl, &pgr};
+#pragma unroll
+  for (int side = 0; side < 2; side++) {
+    const double* q = qs[side];
+    double* F = Fs[side];
+    const double ri = rcp_pos(q[0]);
+    const double u = ri * q[1], v = ri * q[2], w = ri * q[3];
+    const double Bx = q[5], By = q[6], Bz = q[7];
+    const double B2 = Bx * Bx + By * By + Bz * Bz;
+    const double p = gm1 * (q[4] - 0.5 * q[0] * (u * u + v * v + w * w) - B2 * 0.5);
+    const double pt = p + 0.5 * B2;
+    const double Vn = u * ux + v * uy;
+    const double Bn = Bx * ux + By * uy;
+    F[0] = q[0] * Vn;
+    F[1] = q[1] * Vn + pt * ux - Bx * Bn;
+    F[2] = q[2] * Vn + pt * uy - By * Bn;
+    F[3] = q[3] * Vn - Bz * Bn;
+    F[4] = (q[4] + pt) * Vn - Bn * (u * Bx + v * By + w * Bz);
+    F[5] = (v * Bx - u * By) * uy;
+    F[6] = (u * By - v * Bx) * ux;
+    F[7] = Bz * Vn - w * Bn;
+    *pg[side] = p;
+    vn[side] = Vn;
+  }
   const double Bx = 0.5 * (ql[5] + qr[5]), By = 0.5 * (ql[6] + qr[6]), Bz = 0.5 * (ql[7] + qr[7]);
   const double irs = rcp_pos(ql[0] + qr[0]);
-  const double ca = gam * (L.p + R.p) * irs;
+  const double ca = gam * (pgl + pgr) * irs;
   const double cd = (Bx * Bx + By * By + Bz * Bz) * (2.0 * irs);
   const double bn = Bx * ux + By * uy;
   const double cn = bn * bn * (2.0 * irs);
   const double cad = ca + cd;
   const double ctmp = sqrt(cad * cad - 4.0 * ca * cn);
   const double cf = sqrt(0.5 * (cad + ctmp));
-  eigv = 0.5 * fabs(L.Vn + R.Vn) + cf;
-  vnl = L.Vn;
+  eigv = 0.5 * fabs(vn[0] + vn[1]) + cf;
 #pragma unroll
-  for (int k = 0; k < 8; k++)
-    emit(k, scale * fma(-eigv, qr[k] - ql[k], rusanov_flux(ql, L, ux, uy, k) + rusanov_flux(qr, R, ux, uy, k)));
+  for (int k = 0; k < 8; k++) Fh[k] = scale * fma(-eigv, qr[k] - ql[k], Fl[k] + Fr[k]);
+  vnl = vn[0];
 }
 
 // Contravariant viscous + resistive + artificial-viscosity flux at one flux point:

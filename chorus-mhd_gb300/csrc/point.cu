@@ -17,13 +17,14 @@ __global__ void k_point_rusanov(int n, double gam, const double* Qfl, const doub
   const double mag = sqrt(n1 * n1 + n2 * n2);
   const int sign_l = sl[i], sign_r = sr[i];
   const double ux = n1 / mag * sign_l, uy = n2 / mag * sign_l;
-  double ql[9], qr[9], vnl, e;
+  double ql[9], qr[9], Fh[8], vnl, e;
   for (int k = 0; k < 9; k++) { ql[k] = Qfl[9 * i + k]; qr[k] = Qfr[9 * i + k]; }
   const double msl = mag * sign_l, ss = (double)(sign_l * sign_r);
-  rusanov_emit(ql, qr, ux, uy, gam, 0.5 * msl, vnl, e, [&](int k, double f) {
-    Fnl[8 * i + k] = f;
-    Fnr[8 * i + k] = times_sign(f, ss);
-  });
+  rusanov_core(ql, qr, ux, uy, gam, 0.5 * msl, Fh, vnl, e);
+  for (int k = 0; k < 8; k++) {
+    Fnl[8 * i + k] = Fh[k];
+    Fnr[8 * i + k] = times_sign(Fh[k], ss);
+  }
   Az[i] = vnl > 0.0 ? ql[8] : qr[8];
   ev[i] = e;
 }
