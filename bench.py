@@ -39,11 +39,21 @@ NX = 512
 N_SOL = 5
 JITTER = 0.15
 SEED = 1
+PROBLEM = "orszag_tang"
+
+# the configurations of the metric: C2 is the default (the largest that fits one GPU and
+# the one the metric is quoted on); C1 and C3 can be timed the same way
+WORKLOADS = {
+    "C2": dict(problem="orszag_tang", nx=512, n=5, jitter=0.15, seed=1),
+    "C1": dict(problem="orszag_tang", nx=64, n=4, jitter=0.0, seed=0),
+    "C3": dict(problem="rotor", nx=256, n=4, jitter=0.1, seed=1),
+}
 
 
 def workload_name():
-    return "orszag_tang_periodic_%dx%d_jitter%.2f_seed%d_p%d_N%d_fp64_rk_s5p3_av" % (NX, NX, JITTER, SEED, N_SOL - 1,
-                                                                                    N_SOL)
+    bc = "periodic" if PROBLEM != "rotor" else "free"
+    return "%s_%s_%dx%d_jitter%.2f_seed%d_p%d_N%d_fp64_rk_s5p3_av" % (PROBLEM, bc, NX, NX, JITTER, SEED, N_SOL - 1,
+                                                                     N_SOL)
 
 METRIC = "DOF*RK-stage/s"
 HBM_FALLBACK = 6800.0
@@ -69,7 +79,7 @@ def measured_peaks():
 
 def make_case(tmp):
     from chorus_mhd import meshgen
-    spec = meshgen.CaseSpec(nx=NX, ny=NX, N=N_SOL, problem="orszag_tang", jitter=JITTER, seed=SEED, steps=200)
+    spec = meshgen.CaseSpec(nx=NX, ny=NX, N=N_SOL, problem=PROBLEM, jitter=JITTER, seed=SEED, steps=200)
     d = os.path.join(tmp, "case")
     meshgen.write_case(spec, d)
     return d
@@ -236,7 +246,8 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered %dx%d periodic mesh, Orszag-Tang initial data)" % (NX, NX),
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded %s %dx%d mesh, jitter %.2f h, %s initial data)" % (
+            "periodic" if PROBLEM != "rotor" else "FREE-boundary", NX, NX, JITTER, PROBLEM),
         "config": {"workload": workload_name(), "cells": nc, "N": N, "dof": dof, "stages_per_step": 5,
                    "l2": "inputs larger than L2 (%.1f GB resident per replica)" % (dev_bytes / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -420,8 +431,11 @@ def run_reference(args):
 
 
 def main():
-    global NX, N_SOL
+    global NX, N_SOL, JITTER, SEED, PROBLEM
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="C2", choices=sorted(WORKLOADS),
+                    help="C2: Orszag-Tang 512^2 jittered N=5 (default); C1: Orszag-Tang 64^2 N=4; "
+                         "C3: rotor 256^2 jittered N=4, FREE boundaries")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -433,10 +447,15 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-requests", type=int, default=24)
     ap.add_argument("--serving-rates", type=float, nargs="+", default=[10.0, 100.0, 500.0])
-    ap.add_argument("--nx", type=int, default=NX, help="cells per side (default: the 512x512 workload)")
-    ap.add_argument("--order-n", type=int, default=N_SOL, help="solution points per direction")
+    ap.add_argument("--nx", type=int, default=None, help="cells per side (default: the workload's)")
+    ap.add_argument("--order-n", type=int, default=None, help="solution points per direction")
     args = ap.parse_args()
-    NX, N_SOL = args.nx, args.order_n
+    w = WORKLOADS[args.workload]
+    PROBLEM, JITTER, SEED = w["problem"], w["jitter"], w["seed"]
+    NX = args.nx if args.nx else w["nx"]
+    N_SOL = args.order_n if args.order_n else w["n"]
+    if args.workload != "C2":  # the ensemble and serving legs belong to the default line
+        args.no_ensemble = args.no_serving = True
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":

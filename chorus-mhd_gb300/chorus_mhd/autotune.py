@@ -35,8 +35,8 @@ def cache_path(gpu_name: str) -> str:
 
 def _smem_bytes(N: int, pass_: str, epb: int) -> int:
     NS, NFP = N * N, 2 * (N + 1) * N
-    per = {"e1": NS * 9 + 2 * NS + NFP * 18, "e2": NFP * 9 + NS * 16,
-           "e3": NFP * 10 + NS * 13, "ct": NFP}[pass_]
+    per = {"e1": NS * 9 + 2 * NS + NFP * 9, "e2": NFP * 9 + NS * 16,
+           "e3": NFP * 10 + NS * 13}[pass_]
     return 8 * (epb * per + 2 * (N + 1) * N)
 
 
@@ -70,7 +70,6 @@ def tune_order(N: int, device: int = 0, cells_per_side: int | None = None, reps:
         s.set_option("threads_" + pass_, th)
         if pass_ == "e2":
             s.set_option("skip_inactive_viscous", 1)
-    best["ct"] = {"epb": best["e3"]["epb"], "threads": best["e3"]["threads"]}
     best["cells"] = side * side
     s.close()
     return best
@@ -122,7 +121,7 @@ def apply(solver, table: dict | None) -> bool:
     t = table.get("orders", {}).get(str(solver.N))
     if not t:
         return False
-    for pass_ in ("e1", "e2", "e3", "ct"):
+    for pass_ in ("e1", "e2", "e3"):  # the CT passes keep their built-in shape
         if pass_ in t:
             solver.set_option("epb_" + pass_, int(t[pass_]["epb"]))
             solver.set_option("threads_" + pass_, int(t[pass_]["threads"]))

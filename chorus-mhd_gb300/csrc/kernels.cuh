@@ -138,9 +138,7 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
   double* sT = sQ + epb * NS * 9;     // [epb][NS]      sensor scratch
   double* sU = sT + epb * NS;         // [epb][NS]
   double* sV = sU + epb * NS;         // [epb][NFP][9]  flux-point values
-  double* sF = sV + epb * NFP * 9;    // [epb][NFP][8]  interior contravariant flux
-  double* sZ = sF + epb * NFP * 8;    // [epb][NFP]     interior A_z
-  double* sL = sZ + epb * NFP;        // Lmat (N+1, N)
+  double* sL = sV + epb * NFP * 9;    // Lmat (N+1, N)
   double* sA = sL + (N + 1) * N;      // AV smoothing operator (N, N)
   {
     // all global traffic of the pass is contiguous block copies (coalesced)
@@ -186,7 +184,9 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
     }
   }
   __syncthreads();
-  // contravariant inviscid flux at the interior flux points only
+  // contravariant inviscid flux at the interior flux points only (face points of Fc and
+  // Azf belong to the face pass), written straight out: consecutive threads take
+  // consecutive interior points, whose 64-byte flux records mostly adjoin
   const double gm1 = s.gam - 1.0;
   for (int t = threadIdx.x; t < cnt * NINT; t += blockDim.x) {
     const int e = t / NINT, fp = interior_fp<N>(t - e * NINT);
@@ -195,29 +195,14 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
     const double sx = s.met[2 * g], sy = s.met[2 * g + 1];
     double F[8];
     iflux_contra(qf, sx, sy, gm1, F);
-    double* fo = sF + (e * NFP + fp) * 8;
+    double* fo = s.Fc + g * 8;
 #pragma unroll
     for (int k = 0; k < 8; k++) fo[k] = F[k];
-    sZ[e * NFP + fp] = qf[8];
+    s.Azf[g] = qf[8];
   }
-  __syncthreads();
   {
-    const size_t g0 = (size_t)e0 * NFP;
-    double* gv = s.Qvf + g0 * 9;
+    double* gv = s.Qvf + (size_t)e0 * NFP * 9;
     for (int i = threadIdx.x; i < cnt * NFP * 9; i += blockDim.x) gv[i] = sV[i];
-    // interior points only: face points of Fc / Azf belong to the face pass
-    double* gf = s.Fc + g0 * 8;
-    for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) {
-      const int fp = (i >> 3) % NFP;
-      const int lidx = fp < NF1 ? fp % (N + 1) : (fp - NF1) / N;
-      if (lidx > 0 && lidx < N) gf[i] = sF[i];
-    }
-    double* gz = s.Azf + g0;
-    for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
-      const int fp = i % NFP;
-      const int lidx = fp < NF1 ? fp % (N + 1) : (fp - NF1) / N;
-      if (lidx > 0 && lidx < N) gz[i] = sZ[i];
-    }
   }
   if (!sensor) {
     if (s.skip)
@@ -605,6 +590,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
     // the state itself is read where it is used (the update is elementwise over the
     // block's contiguous state)
     const double* fi = s.Fc + (size_t)e0 * NFP * 8;
+#pragma unroll 4
     for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) sF[i] = -fi[i];
     for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sJ[i] = s.invJ[(size_t)e0 * NS + i];
     for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
@@ -704,6 +690,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
   {
     const size_t g0 = (size_t)e0 * NS * 9;
     const int n = cnt * NS * 9;
+#pragma unroll 4
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const size_t g = g0 + i;
       const double q = s.Q[g], r = sR[i];
@@ -746,48 +733,75 @@ __global__ void __launch_bounds__(256) k_e3(SolveDev s, RKStage rk, int epb, int
 // ---------------------------------------------------------------------------
 template <int N, class O>
 __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt, int epb, int mode, double* sm) {
-  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
-
-  double* sA = sm;  // mode 0: [epb][NS] A_z at solution points; mode 2: [epb][NFP]
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
+  // A_z traces live twice: in Qvf variable 9 (the reference's Qvfi(9)/Qvfj(9), which
+  // nablaQsp(9,9) reads) and compactly in Azf, which the gradient below reads coalesced
   if (mode == 0) {
+    double* sA = sm;  // [epb][NS] A_z at the solution points
     for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sA[i] = s.Q[((size_t)e0 * NS + i) * 9 + 8];
     __syncthreads();
-    for (int t = threadIdx.x; t < cnt * NFP; t += blockDim.x) {
-      const int e = t / NFP, fp = t - e * NFP;
-      const double* a = sA + e * NS;
-      double v = 0.0;
-      if (fp < NF1) {
-        const int ifp = fp % (N + 1), jfp = fp / (N + 1);
+    // one (cell, line) per thread, the mirror symmetry of the points as in E1
+    for (int t = threadIdx.x; t < cnt * 2 * N; t += blockDim.x) {
+      const int e = t / (2 * N), line = t - e * 2 * N;
+      const bool fam1 = line < N;
+      const int ln = fam1 ? line : line - N;
+      const double* qb = sA + e * NS + (fam1 ? ln * N : ln);
+      const int qs = fam1 ? 1 : N;
+      const int f0 = fam1 ? ln * (N + 1) : NF1 + ln, fs = fam1 ? 1 : N;
+      const size_t g0 = (size_t)(e0 + e) * NFP;
+      double v[N];
 #pragma unroll
-        for (int sp = 0; sp < N; sp++) v += a[jfp * N + sp] * O::ops().L[ifp + (N + 1) * sp];
-      } else {
-        const int r = fp - NF1, ifp = r % N, jfp = r / N;
+      for (int sp = 0; sp < N; sp++) v[sp] = qb[sp * qs];
+      double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
 #pragma unroll
-        for (int sp = 0; sp < N; sp++) v += a[sp * N + ifp] * O::ops().L[jfp + (N + 1) * sp];
+      for (int j = 0; j < N / 2; j++) {
+        ev[j] = v[j] + v[N - 1 - j];
+        od[j] = v[j] - v[N - 1 - j];
       }
-      s.Qvf[((size_t)(e0 + e) * NFP + fp) * 9 + 8] = v;
+#pragma unroll
+      for (int f = 0; f <= N / 2; f++) {
+        double E = (N & 1) ? O::ops().LMID[f] * v[(N - 1) / 2] : 0.0;
+        double Od = 0.0;
+#pragma unroll
+        for (int j = 0; j < N / 2; j++) {
+          E += O::ops().CE[f * kHalfS + j] * ev[j];
+          Od += O::ops().CO[f * kHalfS + j] * od[j];
+        }
+        const size_t ga = g0 + f0 + f * fs, gb = g0 + f0 + (N - f) * fs;
+        s.Qvf[ga * 9 + 8] = E + Od;
+        s.Azf[ga] = E + Od;
+        if (f != N - f) {
+          s.Qvf[gb * 9 + 8] = E - Od;
+          s.Azf[gb] = E - Od;
+        }
+      }
     }
   } else {
-    for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) sA[i] = s.Qvf[((size_t)e0 * NFP + i) * 9 + 8];
+    // nablaQsp(9,9) (compflux.f90:107-157): (1/J) sum_r Mmat (A_z S) over both line
+    // families, one (cell, point, component) per thread; then update_B
+    // (magnetic_potential.f90:44-67): B = B0 + curl A_z
+    double* sZ = sm;  // [epb][NFP][2] A_z * (S_x, S_y)
+    for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
+      const size_t g = (size_t)e0 * NFP + i;
+      const double z = s.Azf[g];
+      sZ[2 * i] = z * s.met[2 * g];
+      sZ[2 * i + 1] = z * s.met[2 * g + 1];
+    }
     __syncthreads();
-    for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
-      const int e = t / NS, p = t - e * NS, is = p % N, js = p / N;
-      const size_t gs = (size_t)(e0 + e) * NS + p;
-      const double* w = s.gco + (size_t)(e0 + e) * NG * NS + p;
-      const double* a = sA + e * NFP;
-      double gx = 0.0, gy = 0.0;
+    for (int t = threadIdx.x; t < cnt * NS * 2; t += blockDim.x) {
+      const int c = t & 1, ep = t >> 1, e = ep / NS, p = ep - e * NS, is = p % N, js = p / N;
+      const double* az = sZ + e * NFP * 2 + c;
+      double a = 0.0;
 #pragma unroll
       for (int r = 0; r <= N; r++) {
-        const double fa = a[js * (N + 1) + r], fb = a[NF1 + r * N + is];
-        gx += w[r * NS] * fa;
-        gx += w[((N + 1) + r) * NS] * fb;
-        gy += w[(2 * (N + 1) + r) * NS] * fa;
-        gy += w[(3 * (N + 1) + r) * NS] * fb;
+        a += O::ops().M[r + (N + 1) * is] * az[(js * (N + 1) + r) * 2];
+        a += O::ops().M[r + (N + 1) * js] * az[(NF1 + r * N + is) * 2];
       }
-      s.nQs[gs * 18 + 8] = gx;
-      s.nQs[gs * 18 + 9 + 8] = gy;
-      s.Q[gs * 9 + 5] = gy + s.B0x;
-      s.Q[gs * 9 + 6] = -gx + s.B0y;
+      const size_t gs = (size_t)e0 * NS + ep;
+      a *= s.invJ[gs];
+      s.nQs[gs * 18 + 9 * c + 8] = a;
+      if (c) s.Q[gs * 9 + 5] = a + s.B0x;    // Bx = dA/dy
+      else s.Q[gs * 9 + 6] = -a + s.B0y;     // By = -dA/dx
     }
   }
 }
@@ -809,9 +823,11 @@ __device__ __forceinline__ void ctface_point(const SolveDev& s, int t) {
   const int4 fc = s.face2[f];
   const size_t gl = (size_t)fc.x * NFP + face_fp<N>(fc.y, nfp);
   const size_t gr = (size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp);
-  const double v = half(s.Qvf[gl * 9 + 8] + s.Qvf[gr * 9 + 8]);
+  const double v = half(s.Azf[gl] + s.Azf[gr]);
   s.Qvf[gl * 9 + 8] = v;
   s.Qvf[gr * 9 + 8] = v;
+  s.Azf[gl] = v;
+  s.Azf[gr] = v;
 }
 
 template <int N>
