@@ -66,6 +66,7 @@ SIGNATURES = {
     "rk_s5p3_gpu": (c_int, [c_void_p, dp]),
     "fivestagerk_gpu": (c_int, [c_void_p, dp]),
     "iterations_gpu": (c_int, [c_void_p, c_int, ip, dp, P(ChorusDiag), c_int, ip]),
+    "chorus_gpu_step_host": (c_int, [c_void_p, dp, dp, c_int, ip, dp, P(ChorusDiag), c_int, ip]),
     "getrusanovflux_gpu": (c_int, [c_int, c_double, dp, dp, dp, dp, dp, dp, ip, ip, dp]),
     "getrusanovflux_noalloc_gpu": (c_int, [c_int, c_double, dp, dp, dp, dp, dp, dp, ip, ip, dp]),
     "getifluxvectors_gpu": (c_int, [c_int, c_double, dp, dp, dp]),

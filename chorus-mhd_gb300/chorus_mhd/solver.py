@@ -232,6 +232,27 @@ class Solver:
         self.diagnostics.extend(out)
         return out
 
+    def step_host(self, Qin: np.ndarray | None, Qout: np.ndarray | None, nsteps: int = 1) -> list[dict]:
+        """nsteps of iterations on a host-resident state: Q is uploaded from Qin before the
+        first step and downloaded into Qout after the last (chorus_gpu_step_host; the copies
+        overlap the kernels chunk by chunk, fully so for pinned arrays)."""
+        for a in (Qin, Qout):
+            if a is not None and (a.dtype != np.float64 or a.size != self.nq or not a.flags.c_contiguous):
+                raise ValueError("Q arrays must be contiguous float64 of %d elements" % self.nq)
+        it = ctypes.c_int32(self.iter)
+        t = ctypes.c_double(self.ctime)
+        cap = nsteps // 10 + 2
+        recs = (ChorusDiag * cap)()
+        nd = ctypes.c_int32(0)
+        check(self.L.chorus_gpu_step_host(self._ctx, _dp(Qin) if Qin is not None else None,
+                                          _dp(Qout) if Qout is not None else None, int(nsteps), ctypes.byref(it),
+                                          ctypes.byref(t), recs, cap, ctypes.byref(nd)))
+        self.iter, self.ctime = it.value, t.value
+        out = [dict(iter=r.iter, ctime=r.ctime, residglob=r.residglob, divBglob=r.divBglob,
+                    eigvmax_g=r.eigvmax_g, epsilon0=r.epsilon0) for r in recs[: min(nd.value, cap)]]
+        self.diagnostics.extend(out)
+        return out
+
     def run(self, maxiter: int | None = None, out_dir: str | None = None, nwrite: int | None = None,
             nre: int = 0) -> list[dict]:
         """The iteration loop of iterations.f90:19-87 up to MAXITER, with its output

@@ -107,13 +107,13 @@ static int ensure_ops(int dev, int N, const double* Lmat, const double* Mmat, co
 // per-N dispatch of the stage launches
 // ---------------------------------------------------------------------------
 struct Dispatch {
-  void (*e1)(const SolveDev&, const Launch&, cudaStream_t, int);
+  void (*e1)(const SolveDev&, const Launch&, cudaStream_t, int, int, int);
   void (*e1ns)(const SolveDev&, const Launch&, cudaStream_t);
   void (*f1)(const SolveDev&, cudaStream_t);
   void (*e2)(const SolveDev&, const Launch&, cudaStream_t);
   void (*f2)(const SolveDev&, cudaStream_t);
   void (*e3)(const SolveDev&, const RKStage&, const Launch&, cudaStream_t);
-  void (*ct)(const SolveDev&, const Launch&, cudaStream_t, int);
+  void (*ct)(const SolveDev&, const Launch&, cudaStream_t, int, int, int);
   void (*nqsp)(const SolveDev&, int, int, cudaStream_t);
   void (*divb)(const SolveDev&, cudaStream_t);
 };
@@ -130,10 +130,10 @@ Launch default_launch(int N, int which) {
   // which: 0 = E1, 1 = E2, 2 = E3, 3 = CT; cells per CTA and threads per CTA as the
   // autotuner picked them on GB300 for N = 3..6; the CT passes take about 128/(2N) cells
   // so that their (cell, line) loop fills the 128 threads
-  static const int epb[kMaxN + 1][4] = {{0}, {0}, {16, 16, 16, 32}, {8, 16, 8, 21}, {4, 2, 4, 16},
-                                        {4, 1, 4, 12}, {4, 4, 2, 10}, {2, 2, 2, 9}, {2, 2, 2, 8}};
+  static const int epb[kMaxN + 1][4] = {{0}, {0}, {16, 16, 16, 32}, {16, 16, 8, 21}, {4, 2, 4, 16},
+                                        {8, 1, 4, 12}, {8, 4, 4, 10}, {2, 2, 2, 9}, {2, 2, 2, 8}};
   static const int thr[kMaxN + 1][4] = {{0}, {0}, {128, 128, 128, 128}, {256, 256, 128, 128}, {128, 64, 128, 128},
-                                        {256, 64, 128, 128}, {256, 256, 128, 128}, {128, 128, 128, 128},
+                                        {256, 64, 128, 128}, {256, 256, 256, 128}, {128, 128, 128, 128},
                                         {128, 128, 128, 128}};
   return Launch{epb[N][which], thr[N][which]};
 }
@@ -145,6 +145,8 @@ using namespace chorus;
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
+constexpr int kHostChunks = 8;  // chunks of a host-state upload / download
+
 struct ChorusCtx {
   int device = 0;
   ChorusDims dims{};
@@ -164,6 +166,9 @@ struct ChorusCtx {
   int skip_option = 1;  // skip viscous work where it is exactly zero (mu = eta0 = 0, no AV)
   int diagnostics = 1;  // norms every tenth step in iterations_gpu
   std::vector<double> Lmat, Mmat, Xs, Xf;
+  // host-state steps: a copy stream and events that chain chunked copies to kernels
+  cudaStream_t cp = nullptr;
+  cudaEvent_t ev[2 * kHostChunks + 1] = {};
 };
 
 namespace chorus {
@@ -270,6 +275,9 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   auto fail = [&](int code) {
     if (c->arena) cudaFree(c->arena);
     if (c->st) cudaStreamDestroy(c->st);
+    if (c->cp) cudaStreamDestroy(c->cp);
+    for (auto& ev : c->ev)
+      if (ev) cudaEventDestroy(ev);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     delete c;
     return code;
@@ -453,8 +461,12 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   s.eig = (unsigned long long*)(A + oeig);
   s.err = (unsigned int*)(A + oerr);
   c->red = (double*)(A + ored);
-  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->cp, cudaStreamNonBlocking) != cudaSuccess)
     return fail(set_err(CHORUS_ECUDA, "stream creation failed"));
+  for (auto& ev : c->ev)
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+      return fail(set_err(CHORUS_ECUDA, "event creation failed"));
   if (cudaMallocHost(&c->h_pinned, 64 * sizeof(double)) != cudaSuccess)
     return fail(set_err(CHORUS_ECUDA, "pinned allocation failed"));
   e = cudaMemsetAsync(c->arena, 0, P.off, c->st);
@@ -485,7 +497,11 @@ int chorus_gpu_free(ChorusCtx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->arena) cudaFree(c->arena);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  if (c->cp) cudaStreamSynchronize(c->cp);
   if (c->st) cudaStreamDestroy(c->st);
+  if (c->cp) cudaStreamDestroy(c->cp);
+  for (auto& ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
   delete c;
   return CHORUS_OK;
 }
@@ -585,7 +601,7 @@ namespace {
 void enqueue_stage(ChorusCtx* c, const RKStage& rk, bool last) {
   const SolveDev& s = c->sd;
   cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st);
-  c->D->e1(s, c->L[0], c->st, last ? 1 : 0);
+  c->D->e1(s, c->L[0], c->st, last ? 1 : 0, 0, -1);
   c->D->f1(s, c->st);
   c->D->e2(s, c->L[1], c->st);
   c->D->f2(s, c->st);
@@ -593,9 +609,9 @@ void enqueue_stage(ChorusCtx* c, const RKStage& rk, bool last) {
 }
 
 void enqueue_ct(ChorusCtx* c) {
-  c->D->ct(c->sd, c->L[3], c->st, 0);
-  c->D->ct(c->sd, c->L[3], c->st, 1);
-  c->D->ct(c->sd, c->L[3], c->st, 2);
+  c->D->ct(c->sd, c->L[3], c->st, 0, 0, -1);
+  c->D->ct(c->sd, c->L[3], c->st, 1, 0, -1);
+  c->D->ct(c->sd, c->L[3], c->st, 2, 0, -1);
 }
 
 RKStage rk_blank() {
@@ -604,13 +620,12 @@ RKStage rk_blank() {
   return r;
 }
 
-// the five stages of RK_S5P3 (iterations.f90:162-217) or FiveStageRk (:92-160);
-// `diag` marks the last stage to accumulate the residual norm
-void enqueue_rk(ChorusCtx* c, bool diag) {
+// the records of the five stages of RK_S5P3 (iterations.f90:162-217) or FiveStageRk
+// (:92-160); `diag` marks the last stage to accumulate the residual norm
+void make_rk(ChorusCtx* c, bool diag, RKStage* r) {
   const SolveDev& s = c->sd;
   const double dt = c->p.dt;
-  RKStage r[5];
-  for (auto& x : r) x = rk_blank();
+  for (int k = 0; k < 5; k++) r[k] = rk_blank();
   if (c->p.k_stage == 5) {
     const double a11 = 0.39175222700392, a21 = 0.44437049406734, a22 = 0.55562950593266, a23 = 0.36841059262959,
                  a31 = 0.6201018513854, a32 = 0.3798981486146, a33 = 0.25189177424738, a41 = 0.17807995410773,
@@ -636,6 +651,11 @@ void enqueue_rk(ChorusCtx* c, bool diag) {
   }
   r[4].diag = diag ? 1 : 0;
   r[4].write_resid = 1;  // the last stage's residual stays available like the reference's resid
+}
+
+void enqueue_rk(ChorusCtx* c, bool diag) {
+  RKStage r[5];
+  make_rk(c, diag, r);
   for (int k = 0; k < 5; k++) enqueue_stage(c, r[k], k == 4);
 }
 
@@ -655,6 +675,55 @@ void enqueue_diag(ChorusCtx* c) {
   c->D->divb(s, c->st);
   launch_reduce_diag(s.diag, s.NC, c->red, c->st);
   k_store_record<<<1, 1, 0, c->st>>>(c->red, c->sd.eig, c->red + 4);
+}
+
+// One step whose state comes from / goes to host memory: the upload of Q runs on the
+// copy stream in chunks of cells, each chunk's E1 of the first stage starting as soon as
+// its cells have arrived; the download follows the last CT pass chunk by chunk.  E1 and
+// that CT pass are cell-local, so the chunks are independent.
+void enqueue_step_host(ChorusCtx* c, bool diag, const double* Qin, double* Qout) {
+  const SolveDev& s = c->sd;
+  const int NC = s.NC;
+  const size_t per = (size_t)s.N * s.N * 9;
+  const int K = std::max(1, std::min(kHostChunks, NC / 1024));
+  auto cut = [&](int i) { return (int)((long long)NC * i / K); };
+  RKStage r[5];
+  make_rk(c, diag, r);
+  cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st);
+  if (Qin) {
+    cudaEventRecord(c->ev[2 * kHostChunks], c->st);  // earlier work on the state is done
+    cudaStreamWaitEvent(c->cp, c->ev[2 * kHostChunks], 0);
+    for (int i = 0; i < K; i++) {
+      const int a = cut(i), b = cut(i + 1);
+      cudaMemcpyAsync(s.Q + a * per, Qin + a * per, (size_t)(b - a) * per * sizeof(double), cudaMemcpyHostToDevice,
+                      c->cp);
+      cudaEventRecord(c->ev[i], c->cp);
+      cudaStreamWaitEvent(c->st, c->ev[i], 0);
+      c->D->e1(s, c->L[0], c->st, 0, a, b);
+    }
+  } else {
+    c->D->e1(s, c->L[0], c->st, 0, 0, -1);
+  }
+  c->D->f1(s, c->st);
+  c->D->e2(s, c->L[1], c->st);
+  c->D->f2(s, c->st);
+  c->D->e3(s, r[0], c->L[2], c->st);
+  for (int k = 1; k < 5; k++) enqueue_stage(c, r[k], k == 4);
+  c->D->ct(s, c->L[3], c->st, 0, 0, -1);
+  c->D->ct(s, c->L[3], c->st, 1, 0, -1);
+  if (Qout) {
+    for (int i = 0; i < K; i++) {
+      const int a = cut(i), b = cut(i + 1);
+      c->D->ct(s, c->L[3], c->st, 2, a, b);
+      cudaEventRecord(c->ev[kHostChunks + i], c->st);
+      cudaStreamWaitEvent(c->cp, c->ev[kHostChunks + i], 0);
+      cudaMemcpyAsync(Qout + a * per, s.Q + a * per, (size_t)(b - a) * per * sizeof(double), cudaMemcpyDeviceToHost,
+                      c->cp);
+    }
+  } else {
+    c->D->ct(s, c->L[3], c->st, 2, 0, -1);
+  }
+  if (diag) enqueue_diag(c);  // reads Q only: it may overlap the download
 }
 
 int build_graphs(ChorusCtx* c) {
@@ -748,8 +817,22 @@ static int one_step(ChorusCtx* c, double* ctime, int k_stage) {
 int rk_s5p3_gpu(ChorusCtx* c, double* ctime) { return one_step(c, ctime, 3); }
 int fivestagerk_gpu(ChorusCtx* c, double* ctime) { return one_step(c, ctime, 5); }
 
+static int run_steps(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime, ChorusDiag* diag, int32_t max_diag,
+                     int32_t* n_diag, const double* Qin, double* Qout);
+
 int iterations_gpu(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime, ChorusDiag* diag, int32_t max_diag,
                    int32_t* n_diag) {
+  return run_steps(c, nsteps, iter, ctime, diag, max_diag, n_diag, nullptr, nullptr);
+}
+
+int chorus_gpu_step_host(ChorusCtx* c, const double* Qin, double* Qout, int32_t nsteps, int32_t* iter, double* ctime,
+                         ChorusDiag* diag, int32_t max_diag, int32_t* n_diag) {
+  if (nsteps < 1) return set_err(CHORUS_EINVAL, "nsteps must be at least 1");
+  return run_steps(c, nsteps, iter, ctime, diag, max_diag, n_diag, Qin, Qout);
+}
+
+static int run_steps(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime, ChorusDiag* diag, int32_t max_diag,
+                     int32_t* n_diag, const double* Qin, double* Qout) {
   if (!c || !iter || nsteps < 0) return set_err(CHORUS_EINVAL, "bad argument");
   if (ctx_device(c)) return CHORUS_ECUDA;
   if (!c->g_step || c->graph_dt != c->p.dt || c->graph_k != c->p.k_stage) {
@@ -787,7 +870,14 @@ int iterations_gpu(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime, C
   for (int s = 0; s < nsteps; s++) {
     *iter = *iter + 1;
     const bool d = c->diagnostics && (*iter % 10) == 1;
-    CK(cudaGraphLaunch(d ? c->g_diag : c->g_step, c->st));
+    const double* qin = s == 0 ? Qin : nullptr;
+    double* qout = s == nsteps - 1 ? Qout : nullptr;
+    if (qin || qout) {
+      enqueue_step_host(c, d, qin, qout);
+      CK(cudaGetLastError());
+    } else {
+      CK(cudaGraphLaunch(d ? c->g_diag : c->g_step, c->st));
+    }
     if (ctime) *ctime = *ctime + c->p.dt;
     if (d) {
       CK(cudaMemcpyAsync(recs + 3 * pending, c->red + 4, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
@@ -803,6 +893,7 @@ int iterations_gpu(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime, C
   int rc = flush();
   if (rc) return rc;
   if (n_diag) *n_diag = nd;
+  if (Qout) CK(cudaStreamSynchronize(c->cp));
   return check_err_flag(c);
 }
 
@@ -833,7 +924,7 @@ int chorus_gpu_profile_stage(ChorusCtx* c, int32_t reps, double* ms) {
   for (int it = 0; it < reps; it++) {
     CK(cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st));
     CK(cudaEventRecord(ev[0], c->st));
-    c->D->e1(s, c->L[0], c->st, 0);
+    c->D->e1(s, c->L[0], c->st, 0, 0, -1);
     CK(cudaEventRecord(ev[1], c->st));
     c->D->f1(s, c->st);
     CK(cudaEventRecord(ev[2], c->st));

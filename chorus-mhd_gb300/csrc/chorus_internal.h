@@ -119,12 +119,13 @@ struct Launch {
 };
 
 // plot != 0: also record the variable-6 sensor (Se6) when AV is on
-template <int N> void launch_e1(const SolveDev& s, const Launch& L, cudaStream_t st, int plot);
+// cells [c0, c1) (c1 < 0: to the end)
+template <int N> void launch_e1(const SolveDev& s, const Launch& L, cudaStream_t st, int plot, int c0 = 0, int c1 = -1);
 template <int N> void launch_f1(const SolveDev& s, cudaStream_t st);
 template <int N> void launch_e2(const SolveDev& s, const Launch& L, cudaStream_t st);
 template <int N> void launch_f2(const SolveDev& s, cudaStream_t st);
 template <int N> void launch_e3(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st);
-template <int N> void launch_ct(const SolveDev& s, const Launch& L, cudaStream_t st, int mode);
+template <int N> void launch_ct(const SolveDev& s, const Launch& L, cudaStream_t st, int mode, int c0 = 0, int c1 = -1);
 template <int N> void launch_nqsp(const SolveDev& s, int v0, int v1, cudaStream_t st);
 template <int N> void launch_divb(const SolveDev& s, cudaStream_t st);
 

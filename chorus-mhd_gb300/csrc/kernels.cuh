@@ -280,11 +280,12 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
   }
 }
 
+// cells [c0, c1) of the solve, epb per CTA
 template <int N>
-__global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor) {
+__global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor, int c0, int c1) {
   extern __shared__ double sm[];
-  const int e0 = blockIdx.x * epb;
-  const int cnt = min(epb, s.NC - e0);
+  const int e0 = c0 + blockIdx.x * epb;
+  const int cnt = min(epb, c1 - e0);
   if (cnt <= 0) return;
   e1_body<N, OpsTU>(s, e0, cnt, epb, sensor, sm);
 }
@@ -807,10 +808,10 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
 }
 
 template <int N>
-__global__ void __launch_bounds__(256) k_ct_elem(SolveDev s, int epb, int mode) {
+__global__ void __launch_bounds__(256) k_ct_elem(SolveDev s, int epb, int mode, int c0, int c1) {
   extern __shared__ double sm[];
-  const int e0 = blockIdx.x * epb;
-  const int cnt = min(epb, s.NC - e0);
+  const int e0 = c0 + blockIdx.x * epb;
+  const int cnt = min(epb, c1 - e0);
   if (cnt <= 0) return;
   ct_elem_body<N, OpsTU>(s, e0, cnt, epb, mode, sm);
 }

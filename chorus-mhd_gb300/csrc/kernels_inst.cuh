@@ -44,12 +44,13 @@ void CHORUS_CAT(upload_ops_n, CHORUS_N)(const OpsN& o) {
 }
 
 template <>
-void launch_e1<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int plot) {
+void launch_e1<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int plot, int c0, int c1) {
   const int sensor = s.artiv ? (plot ? 3 : 1) : 0;
-  k_e1<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, sensor);
+  if (c1 < 0) c1 = s.NC;
+  if (c1 > c0) k_e1<kN><<<grid_cells(c1 - c0, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, sensor, c0, c1);
 }
 void CHORUS_CAT(launch_e1_nosensor_n, CHORUS_N)(const SolveDev& s, const Launch& L, cudaStream_t st) {
-  k_e1<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, 0);
+  k_e1<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, 0, 0, s.NC);
 }
 template <>
 void launch_f1<kN>(const SolveDev& s, cudaStream_t st) {
@@ -82,12 +83,13 @@ void launch_e3<kN>(const SolveDev& s, const RKStage& rk, const Launch& L, cudaSt
   k_e3<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e3(L.epb), st>>>(s, rk, L.epb, update);
 }
 template <>
-void launch_ct<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int mode) {
+void launch_ct<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int mode, int c0, int c1) {
   if (mode == 1) {
     const int n = s.nface2 * kN;
     if (n > 0) k_ct_face<kN><<<(n + 255) / 256, 256, 0, st>>>(s);
   } else {
-    k_ct_elem<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_ct(L.epb), st>>>(s, L.epb, mode);
+    if (c1 < 0) c1 = s.NC;
+    if (c1 > c0) k_ct_elem<kN><<<grid_cells(c1 - c0, L.epb), L.threads, smem_ct(L.epb), st>>>(s, L.epb, mode, c0, c1);
   }
 }
 template <>

@@ -134,6 +134,16 @@ int fivestagerk_gpu(ChorusCtx* ctx, double* ctime);
  * The whole step is replayed from a CUDA graph. */
 int iterations_gpu(ChorusCtx* ctx, int32_t nsteps, int32_t* iter, double* ctime, ChorusDiag* diag,
                    int32_t max_diag, int32_t* n_diag);
+/* iterations_gpu on a state that lives in host memory, as the reference's own Q does
+ * (setup2d.f90:54): Q(9,N,N,NCELL) is read from Qin before the first step and written to
+ * Qout after the last one (either may be NULL; they may be the same buffer).  The upload
+ * runs in chunks of cells on a second stream, each chunk's first residual pass starting
+ * as soon as its cells have arrived, and the download follows the CT projection chunk by
+ * chunk, so the copies overlap the kernels; with pinned host memory the overlap is full,
+ * pageable memory is accepted and copied synchronously.  No counterpart in the
+ * reference (its Q never leaves the host). */
+int chorus_gpu_step_host(ChorusCtx* ctx, const double* Qin, double* Qout, int32_t nsteps, int32_t* iter,
+                         double* ctime, ChorusDiag* diag, int32_t max_diag, int32_t* n_diag);
 
 /* Point functions with the reference argument lists, evaluated on the device over n
  * points (host arrays, row i at offset i*stride): getrusanov.f90:1-109, :111-153,
