@@ -82,7 +82,9 @@ class Mesh:
 class Plot:
     """Plot output of one solve (tecplotter2dsetup / tecplotter2d / tecpost_parallel):
     the plot-node topology is built once; values() evaluates the nodes on the device,
-    write() also writes the reference's Tecplot binary file."""
+    write() also writes the reference's Tecplot binary file.  With AV on, the solve's
+    latest step (or compresid) must have run with the plot_sensor option set, which
+    records the sensor behind etaAV (Solver.run does this for its output steps)."""
 
     def __init__(self, solver: "Solver", nre: int = 0):
         self.L = solver.L
@@ -271,7 +273,15 @@ class Solver:
                     k = self.iter + 1
                     r = (1 - k) % nwrite
                     nxt = min(maxiter, k + r)
-                recs += self.iterations(nxt - self.iter)
+                if out_dir:
+                    # the step before an output records the sensor that the plot's etaAV needs
+                    if nxt - self.iter > 1:
+                        recs += self.iterations(nxt - self.iter - 1)
+                    self.set_option("plot_sensor", 1)
+                    recs += self.iterations(1)
+                    self.set_option("plot_sensor", 0)
+                else:
+                    recs += self.iterations(nxt - self.iter)
                 if out_dir and ((nwrite > 1 and self.iter % nwrite == 1) or self.iter >= maxiter):
                     plot.write(out_dir)
                     self.write_restart(os.path.join(out_dir, "restart.%08d.dat" % self.iter))

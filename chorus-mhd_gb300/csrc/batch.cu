@@ -86,7 +86,8 @@ __global__ void __launch_bounds__(128) kb_e1(BatchDev b, int slot, int sensor_on
   for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
     const int4 T = b.ctiles[ti];
     const SolveDev& s = load_solve(b.solves + T.x);
-    const int sensor = s.artiv ? sensor_on : 0;  // 1: variable-1 sensor; 3: also variable 6
+    // 1: variable-1 sensor; 3: also variable 6 when the solve's plot flag is set
+    const int sensor = s.artiv ? ((sensor_on & 2) && !*s.plot_flag ? 1 : sensor_on) : 0;
 #define CALL(n) e1_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sensor, sm)
     CHORUS_BATCH_SWITCH(T.w, CALL)
 #undef CALL

@@ -165,6 +165,8 @@ struct ChorusCtx {
   const Dispatch* D = nullptr;
   int skip_option = 1;  // skip viscous work where it is exactly zero (mu = eta0 = 0, no AV)
   int diagnostics = 1;  // norms every tenth step in iterations_gpu
+  int plot_sensor = 0;  // the last stage records the variable-6 sensor (plot etaAV)
+  int se6_valid = 0;    // ... and did so in the latest residual evaluation
   std::vector<double> Lmat, Mmat, Xs, Xf;
   // host-state steps: a copy stream and events that chain chunked copies to kernels
   cudaStream_t cp = nullptr;
@@ -178,6 +180,7 @@ int ctx_device_of(const ChorusCtx* c) { return c->device; }
 double ctx_dt(const ChorusCtx* c) { return c->p.dt; }
 int ctx_kstage(const ChorusCtx* c) { return c->p.k_stage; }
 int ctx_epb(const ChorusCtx* c, int pass) { return c->L[pass].epb; }
+bool ctx_plot_ready(const ChorusCtx* c) { return c->se6_valid != 0 || !c->sd.artiv; }
 static bool g_ops_all_done[64][kMaxN + 1];
 void ensure_ops_all(int dev, int N, const ChorusCtx* c) {
   std::lock_guard<std::mutex> lk(g_ops_mu);
@@ -460,6 +463,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   s.skip = (params->mu == 0.0 && params->eta0 == 0.0) ? 1 : 0;
   s.eig = (unsigned long long*)(A + oeig);
   s.err = (unsigned int*)(A + oerr);
+  s.plot_flag = (const int*)(s.err + 1);  // zeroed with the arena
   c->red = (double*)(A + ored);
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->cp, cudaStreamNonBlocking) != cudaSuccess)
@@ -532,6 +536,10 @@ int chorus_gpu_set_option(ChorusCtx* c, const char* name, int64_t value) {
   std::string n(name);
   if (n == "diagnostics") {
     c->diagnostics = value ? 1 : 0;
+  } else if (n == "plot_sensor") {
+    c->plot_sensor = value ? 1 : 0;
+    CK(cudaMemsetAsync((void*)c->sd.plot_flag, c->plot_sensor, sizeof(int), c->st));
+    return CHORUS_OK;  // read by the kernels at run time: the graphs stay valid
   } else if (n == "skip_inactive_viscous") {
     c->skip_option = value ? 1 : 0;
     c->sd.skip = (c->skip_option && c->p.mu == 0.0 && c->p.eta0 == 0.0) ? 1 : 0;
@@ -562,6 +570,7 @@ int64_t chorus_gpu_get_option(ChorusCtx* c, const char* name) {
   std::string n(name);
   if (n == "skip_inactive_viscous") return c->skip_option;
   if (n == "diagnostics") return c->diagnostics;
+  if (n == "plot_sensor") return c->plot_sensor;
   if (n == "skip_active") return c->sd.skip;
   const char* pass[4] = {"e1", "e2", "e3", "ct"};
   for (int i = 0; i < 4; i++) {
@@ -771,6 +780,7 @@ int compresid_gpu(ChorusCtx* c) {
   RKStage r = rk_blank();
   r.write_resid = 1;
   enqueue_stage(c, r, true);
+  c->se6_valid = c->plot_sensor;
   CK(cudaGetLastError());
   return check_err_flag(c);
 }
@@ -809,6 +819,7 @@ static int one_step(ChorusCtx* c, double* ctime, int k_stage) {
   if (c->p.k_stage != k_stage) return set_err(CHORUS_EINVAL, "context was bound with k_stage=%d", c->p.k_stage);
   if (ctx_device(c)) return CHORUS_ECUDA;
   enqueue_rk(c, false);
+  c->se6_valid = c->plot_sensor;
   CK(cudaGetLastError());
   advance_ctime(k_stage, c->p.dt, ctime);
   return check_err_flag(c);
@@ -893,6 +904,7 @@ static int run_steps(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime,
   int rc = flush();
   if (rc) return rc;
   if (n_diag) *n_diag = nd;
+  if (nsteps > 0) c->se6_valid = c->plot_sensor;
   if (Qout) CK(cudaStreamSynchronize(c->cp));
   return check_err_flag(c);
 }

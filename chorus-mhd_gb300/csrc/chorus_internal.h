@@ -76,7 +76,7 @@ struct SolveDev {
   const double* gco;
   const double* invJ;
   double* Se;
-  double* Se6;                  // the same sum for variable 6 (last stage only; plot output)
+  double* Se6;                  // the same sum for variable 6 (last stage, when plot_flag is set)
   double* muf;
   const int4* face2;            // (cL, lfL, cR, lfR): cells 0-based, local faces 1..4
   const FaceNorm* fn2;          // [face][nfp]
@@ -93,7 +93,7 @@ struct SolveDev {
   unsigned long long* eig;      // bit pattern of the stage's max wave speed (>= 0)
   unsigned int* err;            // error flags (bit 0: non-finite wave speed)
   double* diag;                 // per-cell diagnostic partial sums [e][2]
-  void* pad2;                   // keeps the size a multiple of 16 bytes
+  const int* plot_flag;         // nonzero: the last stage records Se6 (read by E1 at run time)
 };
 
 // One RK stage update: Qnew = sum_j c[j]*src[j] + cQ*Q + cR*R (+ cR0*R0), with

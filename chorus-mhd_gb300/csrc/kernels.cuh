@@ -287,6 +287,7 @@ __global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor, int
   const int e0 = c0 + blockIdx.x * epb;
   const int cnt = min(epb, c1 - e0);
   if (cnt <= 0) return;
+  if ((sensor & 2) && !*s.plot_flag) sensor &= 1;  // the plot's sensor only when asked for
   e1_body<N, OpsTU>(s, e0, cnt, epb, sensor, sm);
 }
 

@@ -29,6 +29,7 @@ namespace chorus {
 int set_err(int code, const char* fmt, ...);
 const SolveDev& ctx_solve(const ChorusCtx* c);
 int ctx_device_of(const ChorusCtx* c);
+bool ctx_plot_ready(const ChorusCtx* c);
 }  // namespace chorus
 
 using namespace chorus;
@@ -334,6 +335,10 @@ int plot_upload(ChorusPlot* P, const double* Xs) {
 // run the node kernels on the solve's stream and wait for them
 int plot_eval(ChorusPlot* P) {
   const SolveDev& s = ctx_solve(P->ctx);
+  if (!ctx_plot_ready(P->ctx))
+    return set_err(CHORUS_ESTATE,
+                   "etaAV needs the variable-6 sensor of the last stage: set the plot_sensor option before the "
+                   "step (or compresid) that precedes the plot");
   PCK(cudaSetDevice(ctx_device_of(P->ctx)));
   cudaStream_t st = (cudaStream_t)chorus_gpu_stream(P->ctx);
   PCK(cudaMemsetAsync(P->d_mm, 0xFF, sizeof(unsigned long long) * 11, st));

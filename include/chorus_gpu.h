@@ -193,6 +193,9 @@ int chorus_gpu_profile_stage(ChorusCtx* ctx, int32_t reps, double* ms);
  *       gradients are needed only within two face rings of an AV-active cell; skip that
  *       work (results are unchanged).  0 computes every cell (and fills every gradient
  *       array for inspection).
+ *   "plot_sensor" (default 0): the last stage of each step also records the AV sensor
+ *       of variable 6, which only the plot output reads (about 1% of a step); takes
+ *       effect on the stream in order, without rebuilding the step graphs;
  *   "epb_e1" / "epb_e2" / "epb_e3" / "epb_ct" (1..64): cells per CTA of a cell pass;
  *   "threads_e1" / ... (32..256, multiple of 32): threads per CTA.
  * chorus_gpu_get_option returns the current value (-1 for an unknown name); the extra
@@ -291,9 +294,11 @@ int chorus_read_restart(ChorusCtx* ctx, const char* path, int32_t* iter, double*
  * (tecplotter2dsetup.f90:1-177) on the host at create, tecplotter2d
  * (tecplotter.f90:1-86) on the device at every evaluation, tecpost_parallel
  * (tecplotter.f90:92-418) as a headless file write.  The node values use the Q of the
- * bound solve and the muAV(1), muAV(6) of its last stage (the sensor of variable 6 is
- * recorded in the last stage of every step and by compresid_gpu).  With ARTIV = 0 the
- * reference never allocates muAV; the muAV/etaAV fields are zeros here.
+ * bound solve and the muAV(1), muAV(6) of its last stage.  muAV(6) needs the sensor of
+ * variable 6, which only the plot reads: the last stage of a step (and compresid_gpu)
+ * records it while the context option "plot_sensor" is 1, so set it before the step that
+ * precedes an output; evaluating a plot otherwise returns CHORUS_ESTATE.  With ARTIV = 0
+ * the reference never allocates muAV; the muAV/etaAV fields are zeros here.
  * --------------------------------------------------------------------------- */
 typedef struct ChorusPlot ChorusPlot;
 /* IVCELL(NCELL,4), IC2F(NCELL,4) 1-based, XV/YV(NVERT), Xs(N) as in the reference;

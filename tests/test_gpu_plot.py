@@ -32,6 +32,7 @@ def same_state(case_root, case, steps=3):
     s = Solver(Mesh(d), initial_state=False)
     s.upload(o.array("Q").copy())
     o.compresid()
+    s.set_option("plot_sensor", 1)
     s.compresid()  # records muAV(1) and muAV(6) of this state, like the oracle's
     return d, o, s
 
@@ -104,4 +105,26 @@ def test_run_writes_on_the_reference_schedule(case_root, tmp_path):
     # names come from ctime with three decimals (several outputs may share one)
     assert 1 <= len(plots) <= 3 and plot_filename(s.ctime) in plots
     assert s.iter == 7
+    s.close()
+
+
+def test_plot_needs_the_sensor_of_the_last_stage(case_root):
+    """etaAV comes from the variable-6 sensor of the latest residual evaluation: without the
+    plot_sensor option on that evaluation the plot is refused rather than stale."""
+    from chorus_mhd import ChorusError
+    d = make_case(case_root, problem="orszag_tang", nx=6, ny=5, N=4, jitter=0.1, seed=3, nre=3)
+    s = Solver(Mesh(d))
+    s.iterations(2)
+    p = s.plot()
+    with pytest.raises(ChorusError):
+        p.values()
+    s.set_option("plot_sensor", 1)
+    s.iterations(1)
+    v = p.values()
+    assert np.isfinite(v["plotQ"]).all()
+    s.set_option("plot_sensor", 0)
+    s.iterations(1)
+    with pytest.raises(ChorusError):
+        p.values()
+    p.close()
     s.close()
