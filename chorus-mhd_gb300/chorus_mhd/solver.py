@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -92,6 +93,9 @@ class Plot:
         h = ctypes.c_void_p()
         check(self.L.chorus_plot_create_mesh(solver._ctx, solver.mesh._h, int(nre), ctypes.byref(h)))
         self._h = h
+        if not hasattr(solver, "_plots"):
+            solver._plots = weakref.WeakSet()
+        solver._plots.add(self)
         n, c, w = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
         check(self.L.chorus_plot_info(self._h, ctypes.byref(n), ctypes.byref(c), ctypes.byref(w)))
         self.nodes, self.cells, self.warned = n.value, c.value, bool(w.value)
@@ -328,6 +332,8 @@ class Solver:
         self.iter, self.ctime = it.value, t.value
 
     def close(self):
+        for p in list(getattr(self, "_plots", ())):  # plots refer to the context
+            p.close()
         if getattr(self, "_ctx", None):
             self.L.chorus_gpu_free(self._ctx)
             self._ctx = None

@@ -883,11 +883,16 @@ static int run_steps(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime,
     const bool d = c->diagnostics && (*iter % 10) == 1;
     const double* qin = s == 0 ? Qin : nullptr;
     double* qout = s == nsteps - 1 ? Qout : nullptr;
-    if (qin || qout) {
+    const size_t qbytes = (size_t)c->dims.NCELL * N * N * 9 * sizeof(double);
+    if ((qin || qout) && qbytes >= ((size_t)64 << 20)) {
+      // large states: copies in chunks, overlapped with the cell-local passes
       enqueue_step_host(c, d, qin, qout);
       CK(cudaGetLastError());
     } else {
+      // small states: the copies take less than the launches a chunked step would add
+      if (qin) CK(cudaMemcpyAsync(c->sd.Q, qin, qbytes, cudaMemcpyHostToDevice, c->st));
       CK(cudaGraphLaunch(d ? c->g_diag : c->g_step, c->st));
+      if (qout) CK(cudaMemcpyAsync(qout, c->sd.Q, qbytes, cudaMemcpyDeviceToHost, c->st));
     }
     if (ctime) *ctime = *ctime + c->p.dt;
     if (d) {

@@ -23,6 +23,9 @@ inline size_t smem_e3(int epb) {
 }
 inline size_t smem_ct(int epb) { return sizeof(double) * epb * D<kN>::NFP * 2; }
 inline int grid_cells(int nc, int epb) { return (nc + epb - 1) / epb; }
+// threads per CTA of a face-point pass: 256, or 64 when that leaves fewer than about
+// eight CTAs per SM (small meshes), so that the points spread over every SM
+inline int face_threads(int n) { return n >= 152 * 8 * 256 ? 256 : 64; }
 
 void set_smem_limits() {
   static bool done[64] = {false};
@@ -55,16 +58,19 @@ void CHORUS_CAT(launch_e1_nosensor_n, CHORUS_N)(const SolveDev& s, const Launch&
 template <>
 void launch_f1<kN>(const SolveDev& s, cudaStream_t st) {
   const int n = (s.nface2 + s.nface1) * kN;
-  if (n > 0) k_f1<kN><<<(n + 255) / 256, 256, 0, st>>>(s);
+  if (n > 0) k_f1<kN><<<(n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st>>>(s);
 }
 template <>
 void launch_e2<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
   // chunks of up to one cell per thread, but small enough for about 16 CTAs per SM
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 152;
+  static int nsm_of[64];  // SM count per device, looked up once
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64) {
+    if (!nsm_of[dev] && (cudaDeviceGetAttribute(&nsm_of[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+                         nsm_of[dev] <= 0))
+      nsm_of[dev] = 152;
+    nsm = nsm_of[dev];
   }
   int chunk = s.NC / (16 * nsm);
   chunk = chunk < L.epb ? L.epb : (chunk > L.threads ? L.threads : chunk);
@@ -75,7 +81,7 @@ void launch_e2<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
 template <>
 void launch_f2<kN>(const SolveDev& s, cudaStream_t st) {
   const int n = (s.nface2 + s.nface1) * kN;
-  if (n > 0) k_f2<kN><<<(n + 255) / 256, 256, 0, st>>>(s);
+  if (n > 0) k_f2<kN><<<(n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st>>>(s);
 }
 template <>
 void launch_e3<kN>(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st) {
@@ -86,7 +92,7 @@ template <>
 void launch_ct<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int mode, int c0, int c1) {
   if (mode == 1) {
     const int n = s.nface2 * kN;
-    if (n > 0) k_ct_face<kN><<<(n + 255) / 256, 256, 0, st>>>(s);
+    if (n > 0) k_ct_face<kN><<<(n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st>>>(s);
   } else {
     if (c1 < 0) c1 = s.NC;
     if (c1 > c0) k_ct_elem<kN><<<grid_cells(c1 - c0, L.epb), L.threads, smem_ct(L.epb), st>>>(s, L.epb, mode, c0, c1);

@@ -306,7 +306,8 @@ typedef struct ChorusPlot ChorusPlot;
 int chorus_plot_create(ChorusCtx* ctx, const int32_t* IVCELL, const int32_t* IC2F, const double* XV,
                        const double* YV, int32_t NVERT, int32_t NFACE, const double* Xs, int32_t NRE,
                        ChorusPlot** plot);
-/* the same from a loaded case; NRE <= 0 takes the case file's NRE */
+/* the same from a loaded case; NRE <= 0 takes the case file's NRE.  A plot refers to
+ * its context: free the plot before the context. */
 int chorus_plot_create_mesh(ChorusCtx* ctx, const ChorusMesh* mesh, int32_t NRE, ChorusPlot** plot);
 int chorus_plot_free(ChorusPlot* plot);
 /* plotnodes, plotcells; warned = 1 where the reference prints its 'something wrong'

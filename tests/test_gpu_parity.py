@@ -146,11 +146,12 @@ def test_skipping_inactive_viscous_work_changes_nothing(case_root, case):
     assert np.array_equal(res[0], res[1])
 
 
-@pytest.mark.parametrize("nsteps", [1, 3, 12])
-def test_step_host_equals_resident_steps(case_root, nsteps):
-    """chorus_gpu_step_host (chunked copies overlapping the passes) gives the same bits as
-    upload + iterations_gpu + download, for pageable and pinned host buffers."""
-    d = make_case(case_root, problem="orszag_tang", nx=72, ny=64, N=4, jitter=0.1, seed=21)
+@pytest.mark.parametrize("nx,ny,nsteps", [(72, 64, 1), (72, 64, 3), (256, 240, 1), (256, 240, 12)])
+def test_step_host_equals_resident_steps(case_root, nx, ny, nsteps):
+    """chorus_gpu_step_host gives the same bits as upload + iterations_gpu + download, for
+    pageable and pinned host buffers: small states (plain copies around the step graph)
+    and states of 64 MB and more (chunked copies overlapping the cell-local passes)."""
+    d = make_case(case_root, problem="orszag_tang", nx=nx, ny=ny, N=4, jitter=0.1, seed=21)
     a = Solver(Mesh(d))
     Q0 = a.state()
     ref_diag = a.iterations(nsteps)
