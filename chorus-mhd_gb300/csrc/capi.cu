@@ -585,6 +585,7 @@ int chorus_gpu_upload_state(ChorusCtx* c, const double* Q) {
   if (ctx_device(c)) return CHORUS_ECUDA;
   const size_t n = (size_t)c->dims.NCELL * c->dims.N * c->dims.N * 9;
   CK(cudaMemcpyAsync(c->sd.Q, Q, n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(c->sd.err, 0, sizeof(unsigned int), c->st));  // a new state: clear its error flags
   CK(cudaStreamSynchronize(c->st));
   return CHORUS_OK;
 }
@@ -878,6 +879,7 @@ static int run_steps(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime,
     diag_times.clear();
     return CHORUS_OK;
   };
+  if (Qin) CK(cudaMemsetAsync(c->sd.err, 0, sizeof(unsigned int), c->st));  // a new state: clear its error flags
   for (int s = 0; s < nsteps; s++) {
     *iter = *iter + 1;
     const bool d = c->diagnostics && (*iter % 10) == 1;

@@ -348,7 +348,9 @@ int mesh_load(const std::string& dir, Mesh& m, std::string& err) {
   // bucket grid with cell size 4*tol; a partner lies at (x +- DX, y) or (x, y +- DY)
   const double cell = 4 * kTolCyc;
   std::unordered_map<int64_t, std::vector<int>> grid;
-  auto gkey = [&](int64_t gx, int64_t gy) { return (gx << 32) ^ (gy & 0xffffffffLL); };
+  auto gkey = [&](int64_t gx, int64_t gy) {  // unsigned shift: the bucket coordinates can be negative
+    return (int64_t)(((uint64_t)gx << 32) ^ ((uint64_t)gy & 0xffffffffULL));
+  };
   for (int i = 0; i < NCY; i++) grid[gkey((int64_t)std::floor(mx[i] / cell), (int64_t)std::floor(my[i] / cell))].push_back(i);
   std::vector<std::vector<int>> partners(NCY);
   const double shifts[4][2] = {{DX, 0}, {-DX, 0}, {0, DY}, {0, -DY}};
