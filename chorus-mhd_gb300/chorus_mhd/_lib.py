@@ -72,6 +72,11 @@ SIGNATURES = {
     "getifluxvectors_gpu": (c_int, [c_int, c_double, dp, dp, dp]),
     "getvfluxvectors_gpu": (c_int, [c_int, c_double, c_double, c_double, dp, dp, dp, dp]),
     "getvfluxvectors_av_gpu": (c_int, [c_void_p, c_int, dp, dp, dp, dp, ip, ip, ip, ip]),
+    "chorus_point_set_params": (c_int, [c_double, c_double, c_double]),
+    "getrusanovflux_c": (c_int, [dp, dp, dp, dp, dp, dp, ip, ip, dp, dp]),
+    "getifluxvectors_c": (c_int, [dp, dp, dp]),
+    "getvfluxvectors_c": (c_int, [dp, dp, dp, dp]),
+    "getvfluxvectors_av_c": (c_int, [c_void_p, dp, dp, dp, dp, ip, ip, ip, ip]),
     "chorus_gpu_stream": (c_void_p, [c_void_p]),
     "chorus_gpu_set_option": (c_int, [c_void_p, c_char_p, ctypes.c_int64]),
     "chorus_gpu_get_option": (ctypes.c_int64, [c_void_p, c_char_p]),

@@ -1150,6 +1150,57 @@ int getvfluxvectors_av_gpu(ChorusCtx* c, int32_t n, const double* Qv, const doub
   return CHORUS_OK;
 }
 
+// single-point forms with the reference's argument lists; the physical constants that
+// the reference reads from module state (gam, mu, eta0: setup2d.f90:68,72,77) come from
+// chorus_point_set_params.  Each evaluates on the device through the n-point entries.
+static std::mutex g_point_mu;
+static double g_point_gam = 5.0 / 3.0, g_point_mu_v = 0.0, g_point_eta0 = 0.0;
+
+int chorus_point_set_params(double gam, double mu, double eta0) {
+  if (!(gam > 1.0) || !(mu >= 0.0) || !(eta0 >= 0.0)) return set_err(CHORUS_EINVAL, "bad point parameters");
+  std::lock_guard<std::mutex> lk(g_point_mu);
+  g_point_gam = gam;
+  g_point_mu_v = mu;
+  g_point_eta0 = eta0;
+  return CHORUS_OK;
+}
+
+static void point_params(double* gam, double* mu, double* eta0) {
+  std::lock_guard<std::mutex> lk(g_point_mu);
+  *gam = g_point_gam;
+  if (mu) *mu = g_point_mu_v;
+  if (eta0) *eta0 = g_point_eta0;
+}
+
+int getrusanovflux_c(const double* Qfl, const double* Qfr, double* Fnl, double* Fnr, double* Az, const double* normf,
+                     const int32_t* sign_l, const int32_t* sign_r, double* eigv, double* eigvmax) {
+  if (!Qfl || !Qfr || !Fnl || !Fnr || !Az || !normf || !sign_l || !sign_r || !eigv || !eigvmax)
+    return set_err(CHORUS_EINVAL, "null argument");
+  double gam;
+  point_params(&gam, nullptr, nullptr);
+  int rc = getrusanovflux_gpu(1, gam, Qfl, Qfr, Fnl, Fnr, Az, normf, sign_l, sign_r, eigv);
+  if (rc) return rc;
+  if (*eigv > *eigvmax) *eigvmax = *eigv;  // getrusanov.f90:105-107
+  return CHORUS_OK;
+}
+
+int getifluxvectors_c(const double* Qi, double* Fi, double* Gi) {
+  double gam;
+  point_params(&gam, nullptr, nullptr);
+  return getifluxvectors_gpu(1, gam, Qi, Fi, Gi);
+}
+
+int getvfluxvectors_c(const double* Qv, const double* nablaQ, double* Fv, double* Gv) {
+  double gam, mu, eta0;
+  point_params(&gam, &mu, &eta0);
+  return getvfluxvectors_gpu(1, gam, mu, eta0, Qv, nablaQ, Fv, Gv);
+}
+
+int getvfluxvectors_av_c(ChorusCtx* ctx, const double* Qv, const double* nablaQ, double* Fv, double* Gv,
+                         const int32_t* fam, const int32_t* ifp, const int32_t* jfp, const int32_t* ic) {
+  return getvfluxvectors_av_gpu(ctx, 1, Qv, nablaQ, Fv, Gv, fam, ifp, jfp, ic);
+}
+
 // ---------------------------------------------------------------------------
 // host-side setup
 // ---------------------------------------------------------------------------

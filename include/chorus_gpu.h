@@ -165,6 +165,22 @@ int getvfluxvectors_gpu(int32_t n, double gam, double mu, double eta0, const dou
 int getvfluxvectors_av_gpu(ChorusCtx* ctx, int32_t n, const double* Qv /*n x 9*/,
                            const double* nablaQ /*n x 18*/, double* Fv /*n x 9*/, double* Gv /*n x 9*/,
                            const int32_t* fam, const int32_t* ifp, const int32_t* jfp, const int32_t* ic);
+/* Single-point forms with the reference's own argument lists (all by reference, as a
+ * Fortran CALL passes them), for unit tests written against the reference routines:
+ * getrusanovflux(Qfl,Qfr,Fnl,Fnr,Az,normf,sign_l,sign_r,eigv) plus the module variable
+ * eigvmax it raises (getrusanov.f90:1-109), getIfluxvectors(Qi,Fi,Gi) (:111-153),
+ * getVfluxvectors(Qv,nablaQ,Fv,Gv) (:157-249), getVfluxvectors_AV(...,fam,ifp,jfp,ic)
+ * (:251-360, with the bound solve standing in for the module's muAVfi/muAVfj).  gam, mu
+ * and eta0, module state in the reference (setup2d.f90:68,72,77), are set process-wide by
+ * chorus_point_set_params (defaults 5/3, 0, 0).  They evaluate on the device. */
+int chorus_point_set_params(double gam, double mu, double eta0);
+int getrusanovflux_c(const double* Qfl, const double* Qfr, double* Fnl, double* Fnr, double* Az,
+                     const double* normf, const int32_t* sign_l, const int32_t* sign_r, double* eigv,
+                     double* eigvmax);
+int getifluxvectors_c(const double* Qi, double* Fi, double* Gi);
+int getvfluxvectors_c(const double* Qv, const double* nablaQ, double* Fv, double* Gv);
+int getvfluxvectors_av_c(ChorusCtx* ctx, const double* Qv, const double* nablaQ, double* Fv, double* Gv,
+                         const int32_t* fam, const int32_t* ifp, const int32_t* jfp, const int32_t* ic);
 /* getrusanovflux_gpu for callers that cannot allocate device memory (no counterpart in
  * the reference): a host whose device memory is all held by its own pool, or one with
  * work in flight that a cudaFree would stall.  Same arguments and results; the device

@@ -135,3 +135,39 @@ def test_vflux_av_points_use_the_solve_face_viscosity(case_root):
     assert L.getvfluxvectors_av_gpu(s._ctx, n, _dp(Q), _dp(G), _dp(Fv), _dp(Gv), _ip(fam), _ip(ifp), _ip(jfp),
                                     _ip(bad)) == 1
     s.close()
+
+
+def test_single_point_forms_with_the_reference_argument_lists():
+    """getrusanovflux_c / getifluxvectors_c / getvfluxvectors_c: one point, arguments by
+    reference as a Fortran CALL passes them, gam/mu/eta0 as module state; eigvmax is
+    raised only by a larger wave speed (getrusanov.f90:105-107)."""
+    L = _lib.load()
+    rng = np.random.default_rng(5)
+    gam, mu, eta0 = 1.4, 0.02, 0.01
+    _lib.check(L.chorus_point_set_params(gam, mu, eta0))
+    try:
+        Q = random_states(rng, 4)
+        nf = rng.normal(size=(4, 2))
+        eigvmax = np.array([0.0])
+        seen = []
+        for i in range(3):
+            Fl, Fr, Az, ev = np.zeros(8), np.zeros(8), np.zeros(1), np.zeros(1)
+            sl, sr = np.array([1], np.int32), np.array([-1 if i % 2 else 1], np.int32)
+            _lib.check(L.getrusanovflux_c(_dp(Q[i]), _dp(Q[i + 1]), _dp(Fl), _dp(Fr), _dp(Az), _dp(nf[i]), _ip(sl),
+                                          _ip(sr), _dp(ev), _dp(eigvmax)))
+            a, b, z, e = oracle.getrusanovflux(gam, Q[i], Q[i + 1], nf[i], sl[0], sr[0])
+            assert np.allclose(Fl, a, rtol=TOL, atol=TOL) and np.allclose(Fr, b, rtol=TOL, atol=TOL)
+            assert Az[0] == z and abs(ev[0] - e) <= TOL * e
+            seen.append(ev[0])
+            assert eigvmax[0] == max(seen)
+        F, G = np.zeros(8), np.zeros(8)
+        _lib.check(L.getifluxvectors_c(_dp(np.ascontiguousarray(Q[0, :8])), _dp(F), _dp(G)))
+        a, b = oracle.getifluxvectors(gam, Q[0, :8])
+        assert np.allclose(F, a, rtol=TOL, atol=TOL) and np.allclose(G, b, rtol=TOL, atol=TOL)
+        g = rng.normal(size=18)
+        Fv, Gv = np.zeros(9), np.zeros(9)
+        _lib.check(L.getvfluxvectors_c(_dp(Q[1]), _dp(g), _dp(Fv), _dp(Gv)))
+        a, b = oracle.getvfluxvectors(gam, mu, eta0, Q[1], g)
+        assert np.allclose(Fv, a, rtol=1e-11, atol=1e-13) and np.allclose(Gv, b, rtol=1e-11, atol=1e-13)
+    finally:
+        _lib.check(L.chorus_point_set_params(5.0 / 3, 0.0, 0.0))
