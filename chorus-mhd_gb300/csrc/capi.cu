@@ -116,9 +116,11 @@ struct Dispatch {
   void (*ct)(const SolveDev&, const Launch&, cudaStream_t, int, int, int);
   void (*nqsp)(const SolveDev&, int, int, cudaStream_t);
   void (*divb)(const SolveDev&, cudaStream_t);
+  void (*diag)(const SolveDev&, const Launch&, cudaStream_t, int);
 };
 #define DISPATCH(n) \
-  Dispatch{launch_e1<n>, launch_e1_nosensor_n##n, launch_f1<n>, launch_e2<n>, launch_f2<n>, launch_e3<n>, launch_ct<n>, launch_nqsp<n>, launch_divb<n>}
+  Dispatch{launch_e1<n>, launch_e1_nosensor_n##n, launch_f1<n>, launch_e2<n>, launch_f2<n>, launch_e3<n>, launch_ct<n>, launch_nqsp<n>, launch_divb<n>, \
+           launch_diag<n>}
 static const Dispatch* dispatch_for(int N) {
   static const Dispatch d[kMaxN + 1] = {Dispatch{}, Dispatch{}, DISPATCH(2), DISPATCH(3), DISPATCH(4),
                                         DISPATCH(5), DISPATCH(6), DISPATCH(7), DISPATCH(8)};
@@ -677,10 +679,11 @@ __global__ void k_store_record(const double* red2, const unsigned long long* eig
 
 // diagnostic of iterations.f90:35-76 on the CT-corrected state
 void enqueue_diag(ChorusCtx* c) {
-  SolveDev s = c->sd;
-  s.eig = c->sd.eig + 1;  // keep the last stage's wave speed for the record
-  c->D->e1ns(s, c->L[0], c->st);
-  c->D->f1(s, c->st);
+  const SolveDev& s = c->sd;
+  // comp_inviscid_flux + nablaQsp(6,7) (iterations.f90:35-36) of which the norms read
+  // only the face-averaged B_x, B_y traces; the record keeps the last stage's wave speed
+  c->D->diag(s, c->L[3], c->st, 0);
+  c->D->diag(s, c->L[3], c->st, 1);
   c->D->nqsp(s, 5, 6, c->st);
   c->D->divb(s, c->st);
   launch_reduce_diag(s.diag, s.NC, c->red, c->st);
@@ -926,7 +929,7 @@ int chorus_gpu_launch_counts(ChorusCtx* c, int32_t* per_step, int32_t* per_diag)
   const int stage = 3 + 2 * nf;         // E1 E2 E3 (+ F1 F2)
   const int ct = 2 + (c->nface2 > 0);   // element passes + face average
   if (per_step) *per_step = 5 * stage + ct;
-  if (per_diag) *per_diag = 1 + nf + 4;  // E1, F1, nablaQsp, divB, reduce, record
+  if (per_diag) *per_diag = 1 + (c->nface2 > 0) + 4;  // B traces, face average, nablaQsp, divB, reduce, record
   return CHORUS_OK;
 }
 

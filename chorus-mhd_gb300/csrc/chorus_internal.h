@@ -126,6 +126,8 @@ template <int N> void launch_e2(const SolveDev& s, const Launch& L, cudaStream_t
 template <int N> void launch_f2(const SolveDev& s, cudaStream_t st);
 template <int N> void launch_e3(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st);
 template <int N> void launch_ct(const SolveDev& s, const Launch& L, cudaStream_t st, int mode, int c0 = 0, int c1 = -1);
+// the diagnostic's B_x, B_y traces: mode 0 interpolation, mode 1 face average
+template <int N> void launch_diag(const SolveDev& s, const Launch& L, cudaStream_t st, int mode);
 template <int N> void launch_nqsp(const SolveDev& s, int v0, int v1, cudaStream_t st);
 template <int N> void launch_divb(const SolveDev& s, cudaStream_t st);
 

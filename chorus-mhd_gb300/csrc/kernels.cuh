@@ -837,6 +837,77 @@ __global__ void __launch_bounds__(256) k_ct_face(SolveDev s) {
   ctface_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// The diagnostic of iterations.f90:35-36 (comp_inviscid_flux, then nablaQsp(6,7) for
+// div B) reads only B_x and B_y at the flux points: interpolate those two variables of
+// the CT-corrected state (mode 0, one (cell, line, variable) per thread, the mirror
+// symmetry of the points as in E1) and average them across the two-sided faces (the face
+// pass below), as interfaceflux/CYCLOCFLUX do (interfaceflux_all.f90:79-91); a FREE face
+// keeps its interior trace (bcflux.f90).
+template <int N, class O>
+__device__ __forceinline__ void diag_interp_body(const SolveDev& s, int e0, int cnt, double* sm) {
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
+  double* sB = sm;  // [cnt][NS][2] B_x, B_y
+  for (int i = threadIdx.x; i < cnt * NS * 2; i += blockDim.x)
+    sB[i] = s.Q[((size_t)e0 * NS + (i >> 1)) * 9 + 5 + (i & 1)];
+  __syncthreads();
+  for (int t = threadIdx.x; t < cnt * 2 * N * 2; t += blockDim.x) {
+    const int v = t & 1, el = t >> 1, e = el / (2 * N), line = el - e * 2 * N;
+    const bool fam1 = line < N;
+    const int ln = fam1 ? line : line - N;
+    const double* qb = sB + (e * NS + (fam1 ? ln * N : ln)) * 2 + v;
+    const int qs = fam1 ? 2 : 2 * N;
+    const int f0 = fam1 ? ln * (N + 1) : NF1 + ln, fs = fam1 ? 1 : N;
+    double* ob = s.Qvf + ((size_t)(e0 + e) * NFP + f0) * 9 + 5 + v;
+    double w[N];
+#pragma unroll
+    for (int sp = 0; sp < N; sp++) w[sp] = qb[sp * qs];
+    double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
+#pragma unroll
+    for (int j = 0; j < N / 2; j++) {
+      ev[j] = w[j] + w[N - 1 - j];
+      od[j] = w[j] - w[N - 1 - j];
+    }
+#pragma unroll
+    for (int f = 0; f <= N / 2; f++) {
+      double E = (N & 1) ? O::ops().LMID[f] * w[(N - 1) / 2] : 0.0;
+      double Od = 0.0;
+#pragma unroll
+      for (int j = 0; j < N / 2; j++) {
+        E += O::ops().CE[f * kHalfS + j] * ev[j];
+        Od += O::ops().CO[f * kHalfS + j] * od[j];
+      }
+      ob[(size_t)f * fs * 9] = E + Od;
+      if (f != N - f) ob[(size_t)(N - f) * fs * 9] = E - Od;
+    }
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_diag_interp(SolveDev s, int epb) {
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  diag_interp_body<N, OpsTU>(s, e0, cnt, sm);
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_diag_face(SolveDev s) {
+  constexpr int NFP = D<N>::NFP;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= s.nface2 * N) return;
+  const int f = t / N, nfp = t - f * N;
+  const int4 fc = s.face2[f];
+  double* a = s.Qvf + ((size_t)fc.x * NFP + face_fp<N>(fc.y, nfp)) * 9 + 5;
+  double* b = s.Qvf + ((size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp)) * 9 + 5;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const double v = half(a[k] + b[k]);
+    a[k] = v;
+    b[k] = v;
+  }
+}
+
 // nablaQsp(v0..v1) (compflux.f90:107-157) from the current Qvf, 0-based variables
 template <int N>
 __global__ void __launch_bounds__(256) k_nqsp(SolveDev s, int v0, int v1) {

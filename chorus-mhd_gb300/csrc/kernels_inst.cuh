@@ -99,6 +99,15 @@ void launch_ct<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int mode
   }
 }
 template <>
+void launch_diag<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int mode) {
+  if (mode == 0) {
+    k_diag_interp<kN><<<grid_cells(s.NC, L.epb), L.threads, sizeof(double) * L.epb * D<kN>::NS * 2, st>>>(s, L.epb);
+  } else {
+    const int n = s.nface2 * kN;
+    if (n > 0) k_diag_face<kN><<<(n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st>>>(s);
+  }
+}
+template <>
 void launch_nqsp<kN>(const SolveDev& s, int v0, int v1, cudaStream_t st) {
   const int n = s.NC * D<kN>::NS;
   k_nqsp<kN><<<(n + 255) / 256, 256, 0, st>>>(s, v0, v1);
