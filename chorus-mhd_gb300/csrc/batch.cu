@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(128) kb_ct(BatchDev b, int slot, int mode) {
   }
 }
 
-// face passes: which = 0 Rusanov (F1), 1 gradient/AV averages (F2), 2 CT average
+// face passes: which = 0 Rusanov (F1), 1 grad Q trace averages (not part of a step), 2 CT average
 __global__ void __launch_bounds__(128) kb_face(BatchDev b, int slot, int which) {
   const int nt = b.ntiles[1];
   for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
@@ -342,8 +342,7 @@ static void batch_enqueue_step(ChorusBatch* b) {
     cudaMemsetAsync(b->d_eig, 0, sizeof(unsigned long long) * 2 * b->cap_solves, b->st);
     kb_e1<<<b->grid_cells, 128, sm, b->st>>>(a, 0, stage == 4 ? 3 : 1);
     kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 1, 0);
-    kb_e2<<<b->grid_cells, 128, sm, b->st>>>(a, 2);
-    kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 3, 1);
+    kb_e2<<<b->grid_cells, 128, sm, b->st>>>(a, 2);  // also the face AV viscosities
     kb_e3<<<b->grid_cells, 128, sm, b->st>>>(a, 4, stage);
   }
   cudaMemsetAsync(b->d_counters, 0, sizeof(int) * kCounterSlots, b->st);

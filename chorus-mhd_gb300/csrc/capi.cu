@@ -222,7 +222,7 @@ static size_t arena_plan_bytes(int N, int NC, int nface2, int nface1, int k_stag
   P.take<double>((size_t)NC * 2); P.take<double>((size_t)NC * 4); P.take<double>((size_t)NC * 2);
   P.take<int4>(nface2 + 1); P.take<int2>(nface1 + 1); P.take<FaceNorm>((size_t)nface2 * N + 1);
   P.take<FaceNorm>((size_t)nface1 * N + 1); P.take<unsigned long long>(4); P.take<unsigned int>(4);
-  P.take<double>(8); P.take<int>(NC); P.take<int>(NC); P.take<int4>(NC);
+  P.take<double>(8); P.take<int>(NC); P.take<int>(NC); P.take<int4>(NC); P.take<int4>(NC);
   return P.off;
 }
 
@@ -322,14 +322,14 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   c->nface2 = (int)f2.size();
   c->nface1 = (int)f1.size();
   // face neighbours per cell (local face 1..4 -> cell across it, -1 at FREE faces)
-  std::vector<int4> nbr(NC, make_int4(-1, -1, -1, -1));
-  auto setn = [&](int cell, int lf, int other) {
-    int* v = reinterpret_cast<int*>(&nbr[cell]);
-    v[lf - 1] = other;
+  std::vector<int4> nbr(NC, make_int4(-1, -1, -1, -1)), nbrlf(NC, make_int4(0, 0, 0, 0));
+  auto setn = [&](int cell, int lf, int other, int olf) {
+    reinterpret_cast<int*>(&nbr[cell])[lf - 1] = other;
+    reinterpret_cast<int*>(&nbrlf[cell])[lf - 1] = olf;
   };
   for (const int4& f : f2) {
-    setn(f.x, f.y, f.z);
-    setn(f.z, f.w, f.x);
+    setn(f.x, f.y, f.z, f.w);
+    setn(f.z, f.w, f.x, f.y);
   }
 
   // ---- derived geometry
@@ -414,7 +414,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
          of2 = P.take<int4>(f2.size() + 1), of1 = P.take<int2>(f1.size() + 1),
          ofn2 = P.take<FaceNorm>(fn2.size() + 1), ofn1 = P.take<FaceNorm>(fn1.size() + 1),
          oeig = P.take<unsigned long long>(4), oerr = P.take<unsigned int>(4), ored = P.take<double>(8),
-         oact = P.take<int>(NC), onv = P.take<int>(NC), onbr = P.take<int4>(NC);
+         oact = P.take<int>(NC), onv = P.take<int>(NC), onbr = P.take<int4>(NC), onbrlf = P.take<int4>(NC);
   c->arena_bytes = P.off;
   if (P.off != arena_plan_bytes(N, NC, c->nface2, c->nface1, params->k_stage))
     return fail(set_err(CHORUS_EINVAL, "internal: arena plan mismatch"));
@@ -461,6 +461,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   s.act = (int*)(A + oact);
   s.nv = (int*)(A + onv);
   s.nbr = (const int4*)(A + onbr);
+  s.nbrlf = (const int4*)(A + onbrlf);
   c->skip_option = 1;
   s.skip = (params->mu == 0.0 && params->eta0 == 0.0) ? 1 : 0;
   s.eig = (unsigned long long*)(A + oeig);
@@ -487,6 +488,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   up((void*)s.fn2, fn2.data(), fn2.size() * sizeof(FaceNorm));
   up((void*)s.fn1, fn1.data(), fn1.size() * sizeof(FaceNorm));
   up((void*)s.nbr, nbr.data(), nbr.size() * sizeof(int4));
+  up((void*)s.nbrlf, nbrlf.data(), nbrlf.size() * sizeof(int4));
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return fail(set_err(CHORUS_ECUDA, "upload failed: %s", cudaGetErrorString(e)));
   int rc = ensure_ops(device, N, Lmat, Mmat, Xs, Xf);
@@ -615,9 +617,8 @@ void enqueue_stage(ChorusCtx* c, const RKStage& rk, bool last) {
   cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st);
   c->D->e1(s, c->L[0], c->st, last ? 1 : 0, 0, -1);
   c->D->f1(s, c->st);
-  c->D->e2(s, c->L[1], c->st);
-  c->D->f2(s, c->st);
-  c->D->e3(s, rk, c->L[2], c->st);
+  c->D->e2(s, c->L[1], c->st);  // also the face AV viscosities
+  c->D->e3(s, rk, c->L[2], c->st);  // averages the grad Q traces where it reads them
 }
 
 void enqueue_ct(ChorusCtx* c) {
@@ -719,7 +720,6 @@ void enqueue_step_host(ChorusCtx* c, bool diag, const double* Qin, double* Qout)
   }
   c->D->f1(s, c->st);
   c->D->e2(s, c->L[1], c->st);
-  c->D->f2(s, c->st);
   c->D->e3(s, r[0], c->L[2], c->st);
   for (int k = 1; k < 5; k++) enqueue_stage(c, r[k], k == 4);
   c->D->ct(s, c->L[3], c->st, 0, 0, -1);
@@ -926,7 +926,7 @@ int64_t chorus_gpu_device_bytes(ChorusCtx* c) { return c ? (int64_t)c->arena_byt
 int chorus_gpu_launch_counts(ChorusCtx* c, int32_t* per_step, int32_t* per_diag) {
   if (!c) return set_err(CHORUS_EINVAL, "null context");
   const int nf = (c->nface2 + c->nface1) > 0 ? 1 : 0;
-  const int stage = 3 + 2 * nf;         // E1 E2 E3 (+ F1 F2)
+  const int stage = 3 + nf;             // E1 E2 E3 (+ F1)
   const int ct = 2 + (c->nface2 > 0);   // element passes + face average
   if (per_step) *per_step = 5 * stage + ct;
   if (per_diag) *per_diag = 1 + (c->nface2 > 0) + 4;  // B traces, face average, nablaQsp, divB, reduce, record
@@ -952,8 +952,7 @@ int chorus_gpu_profile_stage(ChorusCtx* c, int32_t reps, double* ms) {
     CK(cudaEventRecord(ev[2], c->st));
     c->D->e2(s, c->L[1], c->st);
     CK(cudaEventRecord(ev[3], c->st));
-    c->D->f2(s, c->st);
-    CK(cudaEventRecord(ev[4], c->st));
+    CK(cudaEventRecord(ev[4], c->st));  // the former F2 pass lives in E2 and E3
     c->D->e3(s, r, c->L[2], c->st);
     CK(cudaEventRecord(ev[5], c->st));
     CK(cudaEventSynchronize(ev[5]));
@@ -1015,6 +1014,9 @@ int chorus_gpu_download_array(ChorusCtx* c, const char* name, double* out, int64
       {"Azfi", s.Azf, 1, 0}, {"Azfj", s.Azf, 1, 1}, {"nablaQvfi", s.nQvf, 18, 0}, {"nablaQvfj", s.nQvf, 18, 1}};
   for (auto& x : split)
     if (n == x.nm) {
+      // the stage averages the grad Q traces where it reads them: store the averages
+      // (idempotent) so that the arrays equal the reference's nablaQvfi / nablaQvfj
+      if (x.p == s.nQvf) c->D->f2(s, c->st);
       const size_t per = (size_t)NF1 * x.w;
       if ((size_t)count != per * NC) return set_err(CHORUS_EINVAL, "%s has %zu elements", name, per * NC);
       int rc = pull(x.p, (size_t)NC * NFP * x.w, h);

@@ -90,10 +90,12 @@ struct SolveDev {
   int* act;
   int* nv;
   const int4* nbr;
+  const int4* nbrlf;            // the neighbour's local face (1..4) across each face, 0 at FREE faces
   unsigned long long* eig;      // bit pattern of the stage's max wave speed (>= 0)
   unsigned int* err;            // error flags (bit 0: non-finite wave speed)
   double* diag;                 // per-cell diagnostic partial sums [e][2]
   const int* plot_flag;         // nonzero: the last stage records Se6 (read by E1 at run time)
+  void* pad3;                   // keeps the size a multiple of 16 bytes
 };
 
 // One RK stage update: Qnew = sum_j c[j]*src[j] + cQ*Q + cR*R (+ cR0*R0), with

@@ -78,6 +78,23 @@ __device__ __forceinline__ int face_fp(int lf, int nfp) {
   }
 }
 
+// the inverse of face_fp: the local face (1..4) of element flux point fp and its
+// position nfp along that face; 0 for an interior flux point
+template <int N>
+__device__ __forceinline__ int fp_face(int fp, int& nfp) {
+  constexpr int NF1 = D<N>::NF1;
+  if (fp < NF1) {
+    const int ifp = fp % (N + 1), jfp = fp / (N + 1);
+    if (ifp == 0) { nfp = N - 1 - jfp; return 4; }
+    if (ifp == N) { nfp = jfp; return 2; }
+    return 0;
+  }
+  const int r = fp - NF1, ifp = r % N, jfp = r / N;
+  if (jfp == 0) { nfp = ifp; return 1; }
+  if (jfp == N) { nfp = N - 1 - ifp; return 3; }
+  return 0;
+}
+
 __device__ __forceinline__ unsigned long long ev_bits(double ev, unsigned int* err) {
   if (!(ev >= 0.0) || ev > 1.0e300) {  // NaN or inf wave speed: non-physical state
     atomicOr(err, 1u);
@@ -396,6 +413,25 @@ __global__ void __launch_bounds__(256) k_f1(SolveDev s) {
 // ---------------------------------------------------------------------------
 // E2: gradients at solution points and their values at every flux point
 // ---------------------------------------------------------------------------
+// the AV viscosity on the four faces of cell c (compAVflux / interfaceAVflux /
+// cyclocAVflux, AV.f90:199-303, 494-564): the mean of the two cells' muAV(1) on a
+// two-sided face (the same bits from either side: the sum commutes), the cell's own on a
+// FREE face; muAV(1) from the stage's sensor and epsilon0 = eigvmax h/(N-1) (AV.f90:147)
+template <int N>
+__device__ __forceinline__ void cell_face_mu(const SolveDev& s, int c) {
+  double m[4] = {0.0, 0.0, 0.0, 0.0};
+  if (s.artiv) {
+    const double eps0 = __longlong_as_double((long long)*s.eig) * s.hmsh / (double)(N - 1) * 1.0;
+    const double mc = av_mu(s.Se[c], eps0);
+    const int4 b = s.nbr[c];
+    const int o[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) m[k] = o[k] >= 0 ? 0.5 * (mc + av_mu(s.Se[o[k]], eps0)) : mc;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) s.muf[4 * c + k] = m[k];
+}
+
 template <int N, class O>
 __device__ __forceinline__ void e2_cells(const SolveDev& s, const int* cells, int n, double* sm) {
   // gradients of the n (<= epb) listed cells; grad A_z (nablaAsp) is computed with the
@@ -483,6 +519,7 @@ __device__ __forceinline__ void e2_cells(const SolveDev& s, const int* cells, in
 template <int N, class O>
 __device__ __forceinline__ void e2_body(const SolveDev& s, int e0, int cnt, int epb, double* sm) {
   __shared__ int list[64];
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) cell_face_mu<N>(s, e0 + e);
   const int nact = active_cells(s, e0, cnt, 0, list);
   if (nact == 0) return;
   for (int i = threadIdx.x; i < nact; i += blockDim.x) list[i] += e0;
@@ -507,7 +544,9 @@ __global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb, int chunk) {
   __shared__ int woff[9];
   const int c0 = blockIdx.x * chunk;
   const int c = c0 + threadIdx.x;
-  const bool need = (int)threadIdx.x < chunk && c < s.NC && needs_gradients(s, c);
+  const bool mine = (int)threadIdx.x < chunk && c < s.NC;
+  if (mine) cell_face_mu<N>(s, c);
+  const bool need = mine && needs_gradients(s, c);
   const unsigned m = __ballot_sync(0xffffffffu, need);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) woff[w + 1] = __popc(m);
@@ -528,42 +567,25 @@ __global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb, int chunk) {
 // ---------------------------------------------------------------------------
 // F2: face-averaged gradients and face AV viscosity
 // ---------------------------------------------------------------------------
+// face averages of the grad Q traces in place (interfaceVISflux, CYCLOCVISFLUX).  The
+// stage itself averages them where the viscous flux reads them (E3); this pass makes the
+// stored traces equal to the reference's nablaQvfi/nablaQvfj when they are downloaded.
 template <int N>
 __device__ __forceinline__ void f2_point(const SolveDev& s, int t) {
   constexpr int NFP = D<N>::NFP;
-  const int n2 = s.nface2 * N, n1 = s.nface1 * N;
-  if (t >= n2 + n1) return;
-  const double eig = __longlong_as_double((long long)*s.eig);
-  const double eps0 = eig * s.hmsh / (double)(N - 1) * 1.0;
-  if (t < n2) {
-    const int f = t / N, nfp = t - f * N;
-    const int4 fc = s.face2[f];
-    const size_t gl = (size_t)fc.x * NFP + face_fp<N>(fc.y, nfp);
-    const size_t gr = (size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp);
-    double* a = s.nQvf + gl * 18;
-    double* b = s.nQvf + gr * 18;
-    const bool live = !s.skip || s.nv[fc.x] || s.nv[fc.z];
+  if (t >= s.nface2 * N) return;
+  const int f = t / N, nfp = t - f * N;
+  const int4 fc = s.face2[f];
+  double* a = s.nQvf + ((size_t)fc.x * NFP + face_fp<N>(fc.y, nfp)) * 18;
+  double* b = s.nQvf + ((size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp)) * 18;
 #pragma unroll
-    for (int d = 0; d < 2 * live; d++)
+  for (int d = 0; d < 2; d++)
 #pragma unroll
-      for (int k = 0; k < 8; k++) {
-        const double v = half(a[9 * d + k] + b[9 * d + k]);
-        a[9 * d + k] = v;
-        b[9 * d + k] = v;
-      }
-    if (nfp == 0) {
-      double m = 0.0;
-      if (s.artiv) m = 0.5 * (av_mu(s.Se[fc.x], eps0) + av_mu(s.Se[fc.z], eps0));
-      s.muf[4 * fc.x + fc.y - 1] = m;
-      s.muf[4 * fc.z + fc.w - 1] = m;
+    for (int k = 0; k < 8; k++) {
+      const double v = half(a[9 * d + k] + b[9 * d + k]);
+      a[9 * d + k] = v;
+      b[9 * d + k] = v;
     }
-  } else if (t < n2 + n1) {
-    const int tt = t - n2, f = tt / N, nfp = tt - f * N;
-    if (nfp == 0) {
-      const int2 fc = s.face1[f];
-      s.muf[4 * fc.x + fc.y - 1] = s.artiv ? av_mu(s.Se[fc.x], eps0) : 0.0;
-    }
-  }
 }
 
 template <int N>
@@ -625,10 +647,26 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
 #pragma unroll
       for (int k = 0; k < 8; k++) q[k] = pq[k];
       q[8] = 0.0;
+      // on a two-sided face the trace of grad Q is the mean of both sides'
+      // (interfaceVISflux / CYCLOCVISFLUX, interfaceflux_all.f90:118-199,
+      // cyclocflux_all.f90:118-208); a FREE face keeps its own (BCVISFLUX)
+      int nfp = 0;
+      const int lf = fp_face<N>(fp, nfp);
+      const int o = lf ? (&s.nbr[c].x)[lf - 1] : -1;
+      if (o >= 0) {
+        const int olf = (&s.nbrlf[c].x)[lf - 1];
+        const double* po = s.nQvf + ((size_t)o * NFP + face_fp<N>(olf, N - 1 - nfp)) * 18;
 #pragma unroll
-      for (int k = 0; k < 8; k++) {
-        gq[k] = pg[k];
-        gq[9 + k] = pg[9 + k];
+        for (int k = 0; k < 8; k++) {
+          gq[k] = half(pg[k] + po[k]);
+          gq[9 + k] = half(pg[9 + k] + po[9 + k]);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          gq[k] = pg[k];
+          gq[9 + k] = pg[9 + k];
+        }
       }
       gq[8] = 0.0;
       gq[17] = 0.0;
