@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(128) kb_face(BatchDev b, int slot, int which) 
 size_t cell_smem_bytes(int N, int epb) {
   const int NS = N * N, NFP = 2 * (N + 1) * N;
   size_t e1 = (size_t)epb * (NS * 9 + 2 * NS + NFP * 9) + (N + 1) * N + N * N;
-  size_t e2 = (size_t)epb * (NFP * 9 + NS * 16) + (N + 1) * N;
+  size_t e2 = (size_t)epb * (NFP * 9 + 4 * (N + 1) * NS + NS * 16);
   size_t e3 = (size_t)epb * (NFP * 8 + NS * (1 + 9 + 1 + 2) + NFP * 2) + (N + 1) * N;
   size_t ct = (size_t)epb * NFP * 2;
   return sizeof(double) * std::max(std::max(e1, e2), std::max(e3, ct));

@@ -435,82 +435,74 @@ __device__ __forceinline__ void cell_face_mu(const SolveDev& s, int c) {
 template <int N, class O>
 __device__ __forceinline__ void e2_cells(const SolveDev& s, const int* cells, int n, double* sm) {
   // gradients of the n (<= epb) listed cells; grad A_z (nablaAsp) is computed with the
-  // divergence in the last pass
+  // divergence in the last pass.  Every loop hands one (cell, point, variable) or (cell,
+  // line, component) item to each thread, so that all lanes issue FP64 work.
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
-  double* sQ = sm;                // [n][NFP][9]
-  double* sG = sQ + n * NFP * 9;  // [n][NS][16]  (d*8 + k)
-  double* sL = sG + n * NS * 16;  // Lmat (N+1, N)
-  {
-    for (int i = threadIdx.x; i < (N + 1) * N; i += blockDim.x) sL[i] = O::ops().L[i];
-    for (int i = threadIdx.x; i < n * NFP * 9; i += blockDim.x) {
-      const int le = i / (NFP * 9), r = i - le * (NFP * 9);
-      sQ[i] = s.Qvf[(size_t)cells[le] * NFP * 9 + r];
-    }
+  double* sQ = sm;                // [n][NFP][9] face-corrected flux-point states
+  double* sW = sQ + n * NFP * 9;  // [n][NG][NS] gradient weights (gco)
+  double* sG = sW + n * NG * NS;  // [n][NS][16] grad Q (d*8 + k)
+  for (int i = threadIdx.x; i < n * NFP * 9; i += blockDim.x) {
+    const int le = i / (NFP * 9), r = i - le * (NFP * 9);
+    sQ[i] = s.Qvf[(size_t)cells[le] * NFP * 9 + r];
+  }
+  for (int i = threadIdx.x; i < n * NG * NS; i += blockDim.x) {
+    const int le = i / (NG * NS), r = i - le * (NG * NS);
+    sW[i] = s.gco[(size_t)cells[le] * NG * NS + r];
   }
   __syncthreads();
-  // grad Q (variables 1-8) at the solution points (nablaQsp)
-  for (int t = threadIdx.x; t < n * NS; t += blockDim.x) {
-    const int le = t / NS, p = t - le * NS, c = cells[le], is = p % N, js = p / N;
-    const size_t gs = (size_t)c * NS + p;
-    const double* w = s.gco + (size_t)c * NG * NS + p;
-    double cx1[N + 1], cx2[N + 1], cy1[N + 1], cy2[N + 1];
+  // grad Q (variables 1-8) at the solution points (nablaQsp): one (cell, point,
+  // variable) per thread, both components
+  for (int t = threadIdx.x; t < n * NS * 8; t += blockDim.x) {
+    const int k = t & 7, lp = t >> 3, le = lp / NS, p = lp - le * NS, is = p % N, js = p / N;
+    const double* w = sW + le * NG * NS + p;
+    const double* q = sQ + le * NFP * 9 + k;
+    double gx = 0.0, gy = 0.0;
 #pragma unroll
     for (int r = 0; r <= N; r++) {
-      cx1[r] = w[r * NS];
-      cx2[r] = w[((N + 1) + r) * NS];
-      cy1[r] = w[(2 * (N + 1) + r) * NS];
-      cy2[r] = w[(3 * (N + 1) + r) * NS];
+      const double a = q[(js * (N + 1) + r) * 9];
+      const double b = q[(NF1 + r * N + is) * 9];
+      gx += w[r * NS] * a;
+      gx += w[((N + 1) + r) * NS] * b;
+      gy += w[(2 * (N + 1) + r) * NS] * a;
+      gy += w[(3 * (N + 1) + r) * NS] * b;
     }
-    const double* q = sQ + le * NFP * 9;
-    double* out = s.nQs + gs * 18;
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-      double gx = 0.0, gy = 0.0;
-#pragma unroll
-      for (int r = 0; r <= N; r++) {
-        const double a = q[(js * (N + 1) + r) * 9 + k];
-        const double b = q[(NF1 + r * N + is) * 9 + k];
-        gx += cx1[r] * a;
-        gx += cx2[r] * b;
-        gy += cy1[r] * a;
-        gy += cy2[r] * b;
-      }
-      out[k] = gx;
-      out[9 + k] = gy;
-      sG[(le * NS + p) * 16 + k] = gx;
-      sG[(le * NS + p) * 16 + 8 + k] = gy;
-    }
+    double* out = s.nQs + ((size_t)cells[le] * NS + p) * 18;
+    out[k] = gx;
+    out[9 + k] = gy;
+    sG[lp * 16 + k] = gx;
+    sG[lp * 16 + 8 + k] = gy;
   }
   __syncthreads();
-  // grad Q at every flux point (nablaQ_interior_FP + face traces)
-  for (int t = threadIdx.x; t < n * NFP; t += blockDim.x) {
-    const int le = t / NFP, fp = t - le * NFP;
-    const double* G = sG + le * NS * 16;
-    double acc[16];
+  // grad Q at every flux point (nablaQ_interior_FP + face traces): one (cell, line,
+  // component) per thread, the mirror symmetry of the points as in E1
+  for (int t = threadIdx.x; t < n * 2 * N * 16; t += blockDim.x) {
+    const int c = t & 15, el = t >> 4, le = el / (2 * N), line = el - le * 2 * N;
+    const bool fam1 = line < N;
+    const int ln = fam1 ? line : line - N;
+    const double* gb = sG + (le * NS + (fam1 ? ln * N : ln)) * 16 + c;
+    const int gs = fam1 ? 16 : N * 16;
+    const int f0 = fam1 ? ln * (N + 1) : NF1 + ln, fs = fam1 ? 1 : N;
+    double* ob = s.nQvf + ((size_t)cells[le] * NFP + f0) * 18 + (c < 8 ? c : c + 1);
+    double v[N];
 #pragma unroll
-    for (int c = 0; c < 16; c++) acc[c] = 0.0;
-    if (fp < NF1) {
-      const int ifp = fp % (N + 1), jfp = fp / (N + 1);
+    for (int sp = 0; sp < N; sp++) v[sp] = gb[sp * gs];
+    double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
 #pragma unroll
-      for (int sp = 0; sp < N; sp++) {
-        const double l = sL[ifp + (N + 1) * sp];
-#pragma unroll
-        for (int c = 0; c < 16; c++) acc[c] += G[(jfp * N + sp) * 16 + c] * l;
-      }
-    } else {
-      const int r = fp - NF1, ifp = r % N, jfp = r / N;
-#pragma unroll
-      for (int sp = 0; sp < N; sp++) {
-        const double l = sL[jfp + (N + 1) * sp];
-#pragma unroll
-        for (int c = 0; c < 16; c++) acc[c] += G[(sp * N + ifp) * 16 + c] * l;
-      }
+    for (int j = 0; j < N / 2; j++) {
+      ev[j] = v[j] + v[N - 1 - j];
+      od[j] = v[j] - v[N - 1 - j];
     }
-    double* o = s.nQvf + ((size_t)cells[le] * NFP + fp) * 18;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      o[k] = acc[k];
-      o[9 + k] = acc[8 + k];
+    for (int f = 0; f <= N / 2; f++) {
+      double E = (N & 1) ? O::ops().LMID[f] * v[(N - 1) / 2] : 0.0;
+      double Od = 0.0;
+#pragma unroll
+      for (int j = 0; j < N / 2; j++) {
+        E += O::ops().CE[f * kHalfS + j] * ev[j];
+        Od += O::ops().CO[f * kHalfS + j] * od[j];
+      }
+      ob[(size_t)f * fs * 18] = E + Od;
+      if (f != N - f) ob[(size_t)(N - f) * fs * 18] = E - Od;
     }
   }
 }
