@@ -38,9 +38,9 @@ void upload_ops_all(int N, const OpsN& o) {
 
 struct BatchDev {
   const SolveDev* solves;   // per slot (eig/err point into the batch's own arrays)
-  const int4* ctiles;       // (slot, e0, cnt, N)
+  const int4* ctiles;       // (slot, e0, cnt, N): the E1, E2, E3 and CT tile lists, one after another
   const int4* ftiles;       // (slot, t0, cnt, N)
-  const int* ntiles;        // [0] cell tiles, [1] face tiles
+  const int* ntiles;        // [0] E1 tiles, [1] face tiles, [2] E2 tiles, [3] E3 tiles, [4] CT tiles
   int* counters;            // per-launch tile counters, zeroed at the start of each stage
   const RKStage* rk;        // [5][cap]
   int cap;
@@ -48,14 +48,6 @@ struct BatchDev {
 };
 
 namespace {
-
-__device__ __forceinline__ int next_tile(int* counter) {
-  __shared__ int t;
-  __syncthreads();
-  if (threadIdx.x == 0) t = atomicAdd(counter, 1);
-  __syncthreads();
-  return t;
-}
 
 __device__ __forceinline__ const SolveDev& load_solve(const SolveDev* src) {
   __shared__ __align__(16) SolveDev ss;
@@ -66,6 +58,34 @@ __device__ __forceinline__ const SolveDev& load_solve(const SolveDev* src) {
   for (int i = threadIdx.x; i < n4; i += blockDim.x) d[i] = a[i];
   __syncthreads();
   return ss;
+}
+
+// Walks a tile list with a persistent CTA: thread 0 claims the next tile with an atomic
+// issued before the current tile's work (its latency overlaps the work), and the solve
+// descriptor is copied to shared memory only when the solve changes.  body(T, s) runs
+// with the whole CTA.
+template <class Body>
+__device__ __forceinline__ void for_each_tile(int* counter, int nt, const int4* tiles, const SolveDev* solves,
+                                              Body&& body) {
+  __shared__ int cur;
+  if (threadIdx.x == 0) cur = atomicAdd(counter, 1);
+  __syncthreads();
+  int ti = cur, slot = -1;
+  const SolveDev* s = nullptr;
+  while (ti < nt) {
+    int nxt = 0;
+    if (threadIdx.x == 0) nxt = atomicAdd(counter, 1);  // consumed after the tile
+    const int4 T = tiles[ti];
+    if (T.x != slot) {
+      s = &load_solve(solves + T.x);  // ends with a barrier
+      slot = T.x;
+    }
+    body(T, *s);
+    __syncthreads();  // every thread is done with this tile
+    if (threadIdx.x == 0) cur = nxt;
+    __syncthreads();
+    ti = cur;
+  }
 }
 
 #define CHORUS_BATCH_SWITCH(NV, CALL) \
@@ -80,75 +100,64 @@ __device__ __forceinline__ const SolveDev& load_solve(const SolveDev* src) {
     default: break;                   \
   }
 
-__global__ void __launch_bounds__(128) kb_e1(BatchDev b, int slot, int sensor_on) {
+// each cell pass walks its own tile list, cut with that pass's cells per CTA
+__global__ void __launch_bounds__(256) kb_e1(BatchDev b, int slot, int sensor_on) {
   extern __shared__ double sm[];
-  const int nt = b.ntiles[0];
-  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
-    const int4 T = b.ctiles[ti];
-    const SolveDev& s = load_solve(b.solves + T.x);
+  for_each_tile(b.counters + slot, b.ntiles[0], b.ctiles, b.solves, [&](const int4& T, const SolveDev& s) {
     // 1: variable-1 sensor; 3: also variable 6 when the solve's plot flag is set
     const int sensor = s.artiv ? ((sensor_on & 2) && !*s.plot_flag ? 1 : sensor_on) : 0;
 #define CALL(n) e1_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sensor, sm)
     CHORUS_BATCH_SWITCH(T.w, CALL)
 #undef CALL
-  }
+  });
 }
 
-__global__ void __launch_bounds__(128) kb_e2(BatchDev b, int slot) {
+__global__ void __launch_bounds__(256) kb_e2(BatchDev b, int slot) {
   extern __shared__ double sm[];
-  const int nt = b.ntiles[0];
-  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
-    const int4 T = b.ctiles[ti];
-    const SolveDev& s = load_solve(b.solves + T.x);
+  for_each_tile(b.counters + slot, b.ntiles[2], b.ctiles + b.ntiles[0], b.solves,
+                [&](const int4& T, const SolveDev& s) {
 #define CALL(n) e2_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sm)
-    CHORUS_BATCH_SWITCH(T.w, CALL)
+                  CHORUS_BATCH_SWITCH(T.w, CALL)
 #undef CALL
-  }
+                });
 }
 
 __global__ void __launch_bounds__(128) kb_e3(BatchDev b, int slot, int stage) {
   extern __shared__ double sm[];
-  const int nt = b.ntiles[0];
-  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
-    const int4 T = b.ctiles[ti];
-    const SolveDev& s = load_solve(b.solves + T.x);
-    const RKStage& rk = b.rk[stage * b.cap + T.x];
+  for_each_tile(b.counters + slot, b.ntiles[3], b.ctiles + b.ntiles[0] + b.ntiles[2], b.solves,
+                [&](const int4& T, const SolveDev& s) {
+                  const RKStage& rk = b.rk[stage * b.cap + T.x];
 #define CALL(n) e3_body<n, OpsAll<n>>(s, T.y, T.z, T.z, rk, 1, sm)
-    CHORUS_BATCH_SWITCH(T.w, CALL)
+                  CHORUS_BATCH_SWITCH(T.w, CALL)
 #undef CALL
-  }
+                });
 }
 
 __global__ void __launch_bounds__(128) kb_ct(BatchDev b, int slot, int mode) {
   extern __shared__ double sm[];
-  const int nt = b.ntiles[0];
-  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
-    const int4 T = b.ctiles[ti];
-    const SolveDev& s = load_solve(b.solves + T.x);
+  for_each_tile(b.counters + slot, b.ntiles[4], b.ctiles + b.ntiles[0] + b.ntiles[2] + b.ntiles[3], b.solves,
+                [&](const int4& T, const SolveDev& s) {
 #define CALL(n) ct_elem_body<n, OpsAll<n>>(s, T.y, T.z, T.z, mode, sm)
-    CHORUS_BATCH_SWITCH(T.w, CALL)
+                  CHORUS_BATCH_SWITCH(T.w, CALL)
 #undef CALL
-  }
+                });
 }
 
 // face passes: which = 0 Rusanov (F1), 1 grad Q trace averages (not part of a step), 2 CT average
 __global__ void __launch_bounds__(128) kb_face(BatchDev b, int slot, int which) {
-  const int nt = b.ntiles[1];
-  for (int ti = next_tile(b.counters + slot); ti < nt; ti = next_tile(b.counters + slot)) {
-    const int4 T = b.ftiles[ti];
-    const SolveDev& s = load_solve(b.solves + T.x);
-    const int t = T.y + threadIdx.x;
-    const bool in = threadIdx.x < T.z;
-    if (which == 0) {
-      unsigned long long evb = 0ull;
-      if (in) {
-#define CALL(n) evb = f1_point<n>(s, t)
+  for_each_tile(b.counters + slot, b.ntiles[1], b.ftiles, b.solves, [&](const int4& T, const SolveDev& s) {
+    // a tile holds 128 to kFaceTileMax points, taken blockDim.x at a time
+    unsigned long long evb = 0ull;
+    for (int base = 0; base < T.z; base += blockDim.x) {
+      const int t = T.y + base + threadIdx.x;
+      if (base + (int)threadIdx.x >= T.z) continue;
+      if (which == 0) {
+        unsigned long long v = 0ull;
+#define CALL(n) v = f1_point<n>(s, t)
         CHORUS_BATCH_SWITCH(T.w, CALL)
 #undef CALL
-      }
-      block_max_ull(evb, s.eig);
-    } else if (in) {
-      if (which == 1) {
+        evb = v > evb ? v : evb;
+      } else if (which == 1) {
 #define CALL(n) f2_point<n>(s, t)
         CHORUS_BATCH_SWITCH(T.w, CALL)
 #undef CALL
@@ -158,16 +167,23 @@ __global__ void __launch_bounds__(128) kb_face(BatchDev b, int slot, int which) 
 #undef CALL
       }
     }
-  }
+    if (which == 0) block_max_ull(evb, s.eig);
+  });
 }
 
-size_t cell_smem_bytes(int N, int epb) {
+// dynamic shared memory of a cell pass (0 E1, 1 E2, 2 E3, 3 CT) on tiles of epb cells:
+// each pass is launched with its own maximum over the batch, so that one pass's large
+// tiles do not cost the others occupancy
+size_t cell_smem_bytes(int N, int epb, int pass) {
   const int NS = N * N, NFP = 2 * (N + 1) * N;
-  size_t e1 = (size_t)epb * (NS * 9 + 2 * NS + NFP * 9) + (N + 1) * N + N * N;
-  size_t e2 = (size_t)epb * (NFP * 9 + 4 * (N + 1) * NS + NS * 16);
-  size_t e3 = (size_t)epb * (NFP * 8 + NS * (1 + 9 + 1 + 2) + NFP * 2) + (N + 1) * N;
-  size_t ct = (size_t)epb * NFP * 2;
-  return sizeof(double) * std::max(std::max(e1, e2), std::max(e3, ct));
+  size_t d = 0;
+  switch (pass) {
+    case 0: d = (size_t)epb * (NS * 9 + 2 * NS + NFP * 9) + (N + 1) * N + N * N; break;
+    case 1: d = (size_t)epb * (NFP * 9 + 4 * (N + 1) * NS + NS * 16); break;
+    case 2: d = (size_t)epb * (NFP * 8 + NS * (1 + 9 + 1 + 2) + NFP * 2) + (N + 1) * N; break;
+    default: d = (size_t)epb * NFP * 2; break;
+  }
+  return sizeof(double) * d;
 }
 
 }  // namespace
@@ -179,7 +195,9 @@ struct BatchSlot {
   ChorusCtx* ctx = nullptr;
   SolveDev sd{};
   int N = 0, NC = 0, nfp_faces = 0;
-  int epb = 4;
+  int epb = 4;             // cells per tile of E3 and the CT passes
+  int epb1 = 4, epb2 = 4;  // ... of E1 and E2
+  int epbct = 4;           // ... of the CT element passes
   double dt = 0.0;
   int k_stage = 3;
   int64_t steps = 0;
@@ -215,14 +233,15 @@ struct ChorusBatch {
   unsigned long long* d_eig = nullptr;
   unsigned int* d_err = nullptr;
   int grid_cells = 0, grid_faces = 0;
-  size_t smem = 0;
+  size_t smem[4] = {0, 0, 0, 0};  // per cell pass: E1, E2, E3, CT
   bool dirty = true;
   cudaGraphExec_t graph = nullptr;
-  size_t graph_smem = 0;
+  size_t graph_smem[4] = {0, 0, 0, 0};
   int ctiles = 0, ftiles = 0;
 };
 
 static constexpr int kCounterSlots = 16;
+static constexpr int kFaceTileMax = 1024;  // face points per tile of the face passes, at most
 
 static int batch_alloc(ChorusBatch* b, int cap_solves, int cap_ctiles, int cap_ftiles) {
   auto fr = [](void* p) { if (p) cudaFree(p); };
@@ -281,13 +300,31 @@ static int batch_rebuild(ChorusBatch* b) {
   std::vector<int4> ct, ft;
   std::vector<int> order(act);
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->slots[a].N > b->slots[c].N; });
-  size_t smem = 0;
+  size_t smem[4] = {0, 0, 0, 0};
+  std::vector<int4> ct2, ct3, ct4;
+  // face tiles: 128 points (one per thread) while the batch is small, up to
+  // kFaceTileMax when there are enough points for about four tiles per CTA
+  long long total_fp = 0;
+  for (int i : order) total_fp += b->slots[i].nfp_faces;
+  int face_tile = (int)std::min<long long>(kFaceTileMax, std::max<long long>(128, total_fp / (4LL * b->grid_faces)));
+  face_tile -= face_tile % 128;
   for (int i : order) {
     const BatchSlot& sl = b->slots[i];
-    for (int e0 = 0; e0 < sl.NC; e0 += sl.epb) ct.push_back(make_int4(i, e0, std::min(sl.epb, sl.NC - e0), sl.N));
-    for (int t0 = 0; t0 < sl.nfp_faces; t0 += 128) ft.push_back(make_int4(i, t0, std::min(128, sl.nfp_faces - t0), sl.N));
-    smem = std::max(smem, cell_smem_bytes(sl.N, sl.epb));
+    for (int e0 = 0; e0 < sl.NC; e0 += sl.epb1) ct.push_back(make_int4(i, e0, std::min(sl.epb1, sl.NC - e0), sl.N));
+    for (int e0 = 0; e0 < sl.NC; e0 += sl.epb2) ct2.push_back(make_int4(i, e0, std::min(sl.epb2, sl.NC - e0), sl.N));
+    for (int e0 = 0; e0 < sl.NC; e0 += sl.epb) ct3.push_back(make_int4(i, e0, std::min(sl.epb, sl.NC - e0), sl.N));
+    for (int e0 = 0; e0 < sl.NC; e0 += sl.epbct) ct4.push_back(make_int4(i, e0, std::min(sl.epbct, sl.NC - e0), sl.N));
+    for (int t0 = 0; t0 < sl.nfp_faces; t0 += face_tile)
+      ft.push_back(make_int4(i, t0, std::min(face_tile, sl.nfp_faces - t0), sl.N));
+    smem[0] = std::max(smem[0], cell_smem_bytes(sl.N, sl.epb1, 0));
+    smem[1] = std::max(smem[1], cell_smem_bytes(sl.N, sl.epb2, 1));
+    smem[2] = std::max(smem[2], cell_smem_bytes(sl.N, sl.epb, 2));
+    smem[3] = std::max(smem[3], cell_smem_bytes(sl.N, sl.epbct, 3));
   }
+  const int n_e1 = (int)ct.size(), n_e2 = (int)ct2.size(), n_e3 = (int)ct3.size(), n_ct = (int)ct4.size();
+  ct.insert(ct.end(), ct2.begin(), ct2.end());
+  ct.insert(ct.end(), ct3.begin(), ct3.end());
+  ct.insert(ct.end(), ct4.begin(), ct4.end());
   const int ns = (int)b->slots.size();
   if (ns > b->cap_solves || (int)ct.size() > b->cap_ctiles || (int)ft.size() > b->cap_ftiles) {
     int rc = batch_alloc(b, std::max(ns * 2, 16), std::max((int)ct.size() * 2, 1024), std::max((int)ft.size() * 2, 1024));
@@ -311,17 +348,21 @@ static int batch_rebuild(ChorusBatch* b) {
     e = cudaMemcpyAsync(b->d_ftiles, ft.data(), sizeof(int4) * ft.size(), cudaMemcpyHostToDevice, b->st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(b->d_rk, rk.data(), sizeof(RKStage) * rk.size(), cudaMemcpyHostToDevice, b->st);
-  int nt[2] = {(int)ct.size(), (int)ft.size()};
+  int nt[5] = {n_e1, (int)ft.size(), n_e2, n_e3, n_ct};
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_ntiles, nt, sizeof nt, cudaMemcpyHostToDevice, b->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
   if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch tables upload: %s", cudaGetErrorString(e));
-  b->ctiles = nt[0];
+  b->ctiles = nt[3];
   b->ftiles = nt[1];
-  if (smem > b->graph_smem && b->graph) {
+  bool grew = false;
+  for (int p = 0; p < 4; p++) {
+    grew = grew || smem[p] > b->graph_smem[p];
+    b->smem[p] = std::max(b->smem[p], smem[p]);
+  }
+  if (grew && b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
-  b->smem = std::max(b->smem, smem);
   b->dirty = false;
   return CHORUS_OK;
 }
@@ -336,19 +377,19 @@ static void batch_enqueue_step(ChorusBatch* b) {
   a.rk = b->d_rk;
   a.cap = b->cap_solves;
   a.pad = 0;
-  const size_t sm = b->smem;
+  const size_t* sm = b->smem;
   for (int stage = 0; stage < 5; stage++) {
     cudaMemsetAsync(b->d_counters, 0, sizeof(int) * kCounterSlots, b->st);
     cudaMemsetAsync(b->d_eig, 0, sizeof(unsigned long long) * 2 * b->cap_solves, b->st);
-    kb_e1<<<b->grid_cells, 128, sm, b->st>>>(a, 0, stage == 4 ? 3 : 1);
+    kb_e1<<<b->grid_cells, 256, sm[0], b->st>>>(a, 0, stage == 4 ? 3 : 1);
     kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 1, 0);
-    kb_e2<<<b->grid_cells, 128, sm, b->st>>>(a, 2);  // also the face AV viscosities
-    kb_e3<<<b->grid_cells, 128, sm, b->st>>>(a, 4, stage);
+    kb_e2<<<b->grid_cells, 256, sm[1], b->st>>>(a, 2);  // also the face AV viscosities
+    kb_e3<<<b->grid_cells, 128, sm[2], b->st>>>(a, 4, stage);
   }
   cudaMemsetAsync(b->d_counters, 0, sizeof(int) * kCounterSlots, b->st);
-  kb_ct<<<b->grid_cells, 128, sm, b->st>>>(a, 5, 0);
+  kb_ct<<<b->grid_cells, 128, sm[3], b->st>>>(a, 5, 0);
   kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 6, 2);
-  kb_ct<<<b->grid_cells, 128, sm, b->st>>>(a, 7, 2);
+  kb_ct<<<b->grid_cells, 128, sm[3], b->st>>>(a, 7, 2);
 }
 
 extern "C" {
@@ -360,7 +401,7 @@ int chorus_batch_create(int32_t device, ChorusBatch** out) {
   ChorusBatch* b = new ChorusBatch();
   b->device = device;
   cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_ntiles, sizeof(int) * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_ntiles, sizeof(int) * 5);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_counters, sizeof(int) * kCounterSlots);
   if (e != cudaSuccess) {
     delete b;
@@ -407,6 +448,9 @@ int chorus_batch_add(ChorusBatch* b, ChorusCtx* ctx, int32_t* slot) {
   sl.NC = sl.sd.NC;
   sl.nfp_faces = (sl.sd.nface2 + sl.sd.nface1) * sl.N;
   sl.epb = std::max(1, std::min(ctx_epb(ctx, 2), 64));
+  sl.epb1 = std::max(1, std::min(ctx_epb(ctx, 0), 64));
+  sl.epb2 = std::max(1, std::min(ctx_epb(ctx, 1), 64));
+  sl.epbct = std::max(1, std::min(ctx_epb(ctx, 3), 64));
   sl.dt = ctx_dt(ctx);
   sl.k_stage = ctx_kstage(ctx);
   sl.active = true;
@@ -451,7 +495,7 @@ int chorus_batch_step(ChorusBatch* b, int32_t nsteps) {
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
     if (e == cudaSuccess) cudaGraphDestroy(g);
     if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch graph: %s", cudaGetErrorString(e));
-    b->graph_smem = b->smem;
+    for (int p = 0; p < 4; p++) b->graph_smem[p] = b->smem[p];
   }
   for (int s = 0; s < nsteps; s++) {
     cudaError_t e = cudaGraphLaunch(b->graph, b->st);

@@ -1058,6 +1058,21 @@ static int dev_copy(T** d, const T* h, size_t n, cudaStream_t st) {
   if (h) CK(cudaMemcpyAsync(*d, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
   return CHORUS_OK;
 }
+// device scratch of one point-function call: every buffer it hands out is freed when the
+// call returns, on every path
+struct DevScratch {
+  std::vector<void*> bufs;
+  template <typename T>
+  int copy(T** d, const T* h, size_t n, cudaStream_t st) {
+    *d = nullptr;
+    const int rc = dev_copy(d, h, n, st);
+    if (*d) bufs.push_back((void*)*d);
+    return rc;
+  }
+  ~DevScratch() {
+    for (void* b : bufs) cudaFree(b);
+  }
+};
 extern "C" {
 
 int getrusanovflux_gpu(int32_t n, double gam, const double* Qfl, const double* Qfr, double* Fnl, double* Fnr,
@@ -1065,14 +1080,15 @@ int getrusanovflux_gpu(int32_t n, double gam, const double* Qfl, const double* Q
   if (n < 0 || (n > 0 && (!Qfl || !Qfr || !Fnl || !Fnr || !Az || !normf || !sign_l || !sign_r || !eigv)))
     return set_err(CHORUS_EINVAL, "bad argument");
   if (n == 0) return CHORUS_OK;
+  DevScratch S;
   double *a, *b, *fl, *fr, *az, *nf, *ev;
   int *sl, *sr;
   cudaStream_t st = 0;
-  int rc = dev_copy(&a, Qfl, 9 * (size_t)n, st) || dev_copy(&b, Qfr, 9 * (size_t)n, st) ||
-           dev_copy<double>(&fl, nullptr, 8 * (size_t)n, st) || dev_copy<double>(&fr, nullptr, 8 * (size_t)n, st) ||
-           dev_copy<double>(&az, nullptr, n, st) || dev_copy(&nf, normf, 2 * (size_t)n, st) ||
-           dev_copy<double>(&ev, nullptr, n, st) || dev_copy(&sl, (const int*)sign_l, n, st) ||
-           dev_copy(&sr, (const int*)sign_r, n, st);
+  int rc = S.copy(&a, Qfl, 9 * (size_t)n, st) || S.copy(&b, Qfr, 9 * (size_t)n, st) ||
+           S.copy<double>(&fl, nullptr, 8 * (size_t)n, st) || S.copy<double>(&fr, nullptr, 8 * (size_t)n, st) ||
+           S.copy<double>(&az, nullptr, n, st) || S.copy(&nf, normf, 2 * (size_t)n, st) ||
+           S.copy<double>(&ev, nullptr, n, st) || S.copy(&sl, (const int*)sign_l, n, st) ||
+           S.copy(&sr, (const int*)sign_r, n, st);
   if (rc) return CHORUS_ECUDA;
   launch_point_rusanov(n, gam, a, b, fl, fr, az, nf, sl, sr, ev, st);
   cudaError_t e = cudaGetLastError();
@@ -1080,8 +1096,6 @@ int getrusanovflux_gpu(int32_t n, double gam, const double* Qfl, const double* Q
   if (e == cudaSuccess) e = cudaMemcpy(Fnr, fr, 8 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(Az, az, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(eigv, ev, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
-  void* ptrs[] = {a, b, fl, fr, az, nf, ev, sl, sr};
-  for (void* p : ptrs) cudaFree(p);
   if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "getrusanovflux_gpu: %s", cudaGetErrorString(e));
   return CHORUS_OK;
 }
@@ -1089,15 +1103,15 @@ int getrusanovflux_gpu(int32_t n, double gam, const double* Qfl, const double* Q
 int getifluxvectors_gpu(int32_t n, double gam, const double* Qi, double* Fi, double* Gi) {
   if (n < 0 || (n > 0 && (!Qi || !Fi || !Gi))) return set_err(CHORUS_EINVAL, "bad argument");
   if (n == 0) return CHORUS_OK;
+  DevScratch S;
   double *q, *f, *g;
-  if (dev_copy(&q, Qi, 8 * (size_t)n, 0) || dev_copy<double>(&f, nullptr, 8 * (size_t)n, 0) ||
-      dev_copy<double>(&g, nullptr, 8 * (size_t)n, 0))
+  if (S.copy(&q, Qi, 8 * (size_t)n, 0) || S.copy<double>(&f, nullptr, 8 * (size_t)n, 0) ||
+      S.copy<double>(&g, nullptr, 8 * (size_t)n, 0))
     return CHORUS_ECUDA;
   launch_point_iflux(n, gam, q, f, g, 0);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpy(Fi, f, 8 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(Gi, g, 8 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
-  cudaFree(q); cudaFree(f); cudaFree(g);
   if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "getifluxvectors_gpu: %s", cudaGetErrorString(e));
   return CHORUS_OK;
 }
@@ -1106,15 +1120,15 @@ int getvfluxvectors_gpu(int32_t n, double gam, double mu, double eta0, const dou
                         double* Fv, double* Gv) {
   if (n < 0 || (n > 0 && (!Qv || !nablaQ || !Fv || !Gv))) return set_err(CHORUS_EINVAL, "bad argument");
   if (n == 0) return CHORUS_OK;
+  DevScratch S;
   double *q, *g, *f, *h;
-  if (dev_copy(&q, Qv, 9 * (size_t)n, 0) || dev_copy(&g, nablaQ, 18 * (size_t)n, 0) ||
-      dev_copy<double>(&f, nullptr, 9 * (size_t)n, 0) || dev_copy<double>(&h, nullptr, 9 * (size_t)n, 0))
+  if (S.copy(&q, Qv, 9 * (size_t)n, 0) || S.copy(&g, nablaQ, 18 * (size_t)n, 0) ||
+      S.copy<double>(&f, nullptr, 9 * (size_t)n, 0) || S.copy<double>(&h, nullptr, 9 * (size_t)n, 0))
     return CHORUS_ECUDA;
   launch_point_vflux(n, gam, mu, eta0, q, g, f, h, 0);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpy(Fv, f, 9 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(Gv, h, 9 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
-  cudaFree(q); cudaFree(g); cudaFree(f); cudaFree(h);
   if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "getvfluxvectors_gpu: %s", cudaGetErrorString(e));
   return CHORUS_OK;
 }
@@ -1125,6 +1139,7 @@ int getvfluxvectors_av_gpu(ChorusCtx* c, int32_t n, const double* Qv, const doub
   if (n < 0 || (n > 0 && (!Qv || !nablaQ || !Fv || !Gv || !fam || !ifp || !jfp || !ic)))
     return set_err(CHORUS_EINVAL, "bad argument");
   if (n == 0) return CHORUS_OK;
+  DevScratch S;
   const int N = c->dims.N, NC = c->dims.NCELL;
   for (int i = 0; i < n; i++) {
     const int f = fam[i], ni = f == 1 ? N + 1 : N, nj = f == 1 ? N : N + 1;
@@ -1139,18 +1154,16 @@ int getvfluxvectors_av_gpu(ChorusCtx* c, int32_t n, const double* Qv, const doub
   double *q, *g, *f, *h;
   int *dfam, *di, *dj, *dc;
   cudaStream_t st = c->st;  // ordered after the context's own work (muf of the last stage)
-  if (dev_copy(&q, Qv, 9 * (size_t)n, st) || dev_copy(&g, nablaQ, 18 * (size_t)n, st) ||
-      dev_copy<double>(&f, nullptr, 9 * (size_t)n, st) || dev_copy<double>(&h, nullptr, 9 * (size_t)n, st) ||
-      dev_copy(&dfam, fam, (size_t)n, st) || dev_copy(&di, ifp, (size_t)n, st) || dev_copy(&dj, jfp, (size_t)n, st) ||
-      dev_copy(&dc, ic, (size_t)n, st))
+  if (S.copy(&q, Qv, 9 * (size_t)n, st) || S.copy(&g, nablaQ, 18 * (size_t)n, st) ||
+      S.copy<double>(&f, nullptr, 9 * (size_t)n, st) || S.copy<double>(&h, nullptr, 9 * (size_t)n, st) ||
+      S.copy(&dfam, fam, (size_t)n, st) || S.copy(&di, ifp, (size_t)n, st) || S.copy(&dj, jfp, (size_t)n, st) ||
+      S.copy(&dc, ic, (size_t)n, st))
     return CHORUS_ECUDA;
   launch_point_vflux_av(n, c->p.gam, ax, c->sd.muf, dfam, di, dj, dc, q, g, f, h, st);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e == cudaSuccess) e = cudaMemcpy(Fv, f, 9 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(Gv, h, 9 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
-  cudaFree(q); cudaFree(g); cudaFree(f); cudaFree(h);
-  cudaFree(dfam); cudaFree(di); cudaFree(dj); cudaFree(dc);
   if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "getvfluxvectors_av_gpu: %s", cudaGetErrorString(e));
   return CHORUS_OK;
 }
