@@ -217,7 +217,7 @@ def run_gpu(args):
                 "frac": gops / FP64_PEAK_GOPS, "unit": "G FP64 instructions/s (thread level)",
                 "ops_per_element_stage": n_ops, "flops_per_element_stage": n_flops,
                 "achieved_tflops": n_flops * nc / (stage_ms / 1e3) / 1e12,
-                "source": "ncu SASS counters of the five stage kernels, Orszag-Tang 262x262 N=5"}
+                "source": "ncu SASS counters of the four stage kernels, Orszag-Tang 262x262 N=5"}
     traffic = None
     if counted and TRAFFIC_PER_ELEMENT_STAGE.get(N):
         traffic = TRAFFIC_PER_ELEMENT_STAGE[N] * nc
@@ -263,7 +263,7 @@ def run_gpu(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the five stage "
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the four stage "
                                        "kernels at 262x262, scaled by cells (bytes per cell are size-independent)",
                      "kernel": "one RK stage (4 launches: %s)" % ", ".join(n for n in names if n),
                      "algorithmic_bytes_per_element_stage": b_stage(N), "peak_kind": peak_kind,
@@ -371,11 +371,11 @@ def run_serving(args, device, tmp):
     return out
 
 
-# per element per RK stage, from ncu on the five stage kernels (Orszag-Tang 262x262,
+# per element per RK stage, from ncu on the four stage kernels (Orszag-Tang 262x262,
 # N=5, after the warm-up steps): FP64 thread instructions (DFMA + DADD + DMUL) and flops
 # (2*DFMA + DADD + DMUL); DRAM bytes read + written
-FP64_PER_ELEMENT_STAGE: dict = {5: (11036, 17671)}
-TRAFFIC_PER_ELEMENT_STAGE: dict = {5: 26552}
+FP64_PER_ELEMENT_STAGE: dict = {5: (10798, 17208)}
+TRAFFIC_PER_ELEMENT_STAGE: dict = {5: 26349}
 
 
 def cpu_baseline(case_dir, dof, warm=1, timed=2):
