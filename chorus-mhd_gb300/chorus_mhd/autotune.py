@@ -21,7 +21,7 @@ from . import meshgen
 
 PASSES = {"e1": 0, "e2": 2, "e3": 4}  # index into profile_stage's per-kernel times
 EPB_CANDIDATES = [1, 2, 4, 8, 16]
-THREAD_CANDIDATES = [64, 128, 256]
+THREAD_CANDIDATES = [64, 128, 192, 256, 384, 512]
 SMEM_LIMIT = 200 * 1024
 
 

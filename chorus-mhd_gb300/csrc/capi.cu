@@ -133,9 +133,9 @@ Launch default_launch(int N, int which) {
   // autotuner picked them on GB300 for N = 3..6; the CT passes take about 128/(2N) cells
   // so that their (cell, line) loop fills the 128 threads
   static const int epb[kMaxN + 1][4] = {{0}, {0}, {16, 16, 16, 32}, {16, 8, 8, 21}, {4, 4, 4, 16},
-                                        {8, 4, 4, 12}, {8, 2, 4, 10}, {2, 2, 2, 9}, {2, 2, 2, 8}};
-  static const int thr[kMaxN + 1][4] = {{0}, {0}, {128, 128, 128, 128}, {256, 256, 128, 128}, {256, 128, 128, 128},
-                                        {256, 256, 128, 128}, {256, 256, 256, 128}, {128, 128, 128, 128},
+                                        {16, 4, 4, 12}, {8, 2, 4, 10}, {2, 2, 2, 9}, {2, 2, 2, 8}};
+  static const int thr[kMaxN + 1][4] = {{0}, {0}, {128, 128, 128, 128}, {192, 384, 128, 128}, {128, 128, 128, 128},
+                                        {512, 384, 128, 128}, {256, 256, 192, 128}, {128, 128, 128, 128},
                                         {128, 128, 128, 128}};
   return Launch{epb[N][which], thr[N][which]};
 }
@@ -559,7 +559,9 @@ int chorus_gpu_set_option(ChorusCtx* c, const char* name, int64_t value) {
       if (value < 1 || value > 64) return set_err(CHORUS_EINVAL, "%s=%lld outside 1..64", name, (long long)value);
       c->L[w].epb = (int)value;
     } else {
-      if (value < 32 || value > 256 || value % 32) return set_err(CHORUS_EINVAL, "%s=%lld must be 32..256, a multiple of 32", name, (long long)value);
+      const int lim = w == 3 ? 256 : 512;  // the kernels' launch bounds
+      if (value < 32 || value > lim || value % 32)
+        return set_err(CHORUS_EINVAL, "%s=%lld must be 32..%d, a multiple of 32", name, (long long)value, lim);
       c->L[w].threads = (int)value;
     }
   } else {

@@ -299,7 +299,7 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
 
 // cells [c0, c1) of the solve, epb per CTA
 template <int N>
-__global__ void __launch_bounds__(256) k_e1(SolveDev s, int epb, int sensor, int c0, int c1) {
+__global__ void __launch_bounds__(512) k_e1(SolveDev s, int epb, int sensor, int c0, int c1) {
   extern __shared__ double sm[];
   const int e0 = c0 + blockIdx.x * epb;
   const int cnt = min(epb, c1 - e0);
@@ -530,10 +530,10 @@ __device__ __forceinline__ bool needs_gradients(const SolveDev& s, int c) {
 // cell, the CTA compacts the cells that need gradients into an ordered list and runs
 // them in groups of epb, so chunks without viscous work cost one coalesced test
 template <int N>
-__global__ void __launch_bounds__(256) k_e2(SolveDev s, int epb, int chunk) {
+__global__ void __launch_bounds__(512) k_e2(SolveDev s, int epb, int chunk) {
   extern __shared__ double sm[];
-  __shared__ int list[256];
-  __shared__ int woff[9];
+  __shared__ int list[512];
+  __shared__ int woff[17];
   const int c0 = blockIdx.x * chunk;
   const int c = c0 + threadIdx.x;
   const bool mine = (int)threadIdx.x < chunk && c < s.NC;
@@ -749,7 +749,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
 }
 
 template <int N>
-__global__ void __launch_bounds__(256) k_e3(SolveDev s, RKStage rk, int epb, int update) {
+__global__ void __launch_bounds__(512) k_e3(SolveDev s, RKStage rk, int epb, int update) {
   extern __shared__ double sm[];
   const int e0 = blockIdx.x * epb;
   const int cnt = min(epb, s.NC - e0);

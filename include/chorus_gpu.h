@@ -213,7 +213,8 @@ int chorus_gpu_profile_stage(ChorusCtx* ctx, int32_t reps, double* ms);
  *       of variable 6, which only the plot output reads (about 1% of a step); takes
  *       effect on the stream in order, without rebuilding the step graphs;
  *   "epb_e1" / "epb_e2" / "epb_e3" / "epb_ct" (1..64): cells per CTA of a cell pass;
- *   "threads_e1" / ... (32..256, multiple of 32): threads per CTA.
+ *   "threads_e1" / "threads_e2" / "threads_e3" (32..512) and "threads_ct" (32..256), multiples of 32:
+ *       threads per CTA.
  * chorus_gpu_get_option returns the current value (-1 for an unknown name); the extra
  * read-only name "skip_active" tells whether skipping is in effect. */
 int chorus_gpu_set_option(ChorusCtx* ctx, const char* name, int64_t value);
