@@ -448,8 +448,10 @@ int chorus_batch_add(ChorusBatch* b, ChorusCtx* ctx, int32_t* slot) {
   sl.NC = sl.sd.NC;
   sl.nfp_faces = (sl.sd.nface2 + sl.sd.nface1) * sl.N;
   sl.epb = std::max(1, std::min(ctx_epb(ctx, 2), 64));
-  sl.epb1 = std::max(1, std::min(ctx_epb(ctx, 0), 64));
-  sl.epb2 = std::max(1, std::min(ctx_epb(ctx, 1), 64));
+  // the batched E1/E2 run 256 threads per CTA: tiles of at most 8 cells keep their
+  // shared memory (and occupancy) in the range the single-solve shapes were tuned for
+  sl.epb1 = std::max(1, std::min(ctx_epb(ctx, 0), 8));
+  sl.epb2 = std::max(1, std::min(ctx_epb(ctx, 1), 8));
   sl.epbct = std::max(1, std::min(ctx_epb(ctx, 3), 64));
   sl.dt = ctx_dt(ctx);
   sl.k_stage = ctx_kstage(ctx);
