@@ -616,8 +616,7 @@ namespace {
 // single compresid), whose E1 also records the variable-6 sensor the plot output reads
 void enqueue_stage(ChorusCtx* c, const RKStage& rk, bool last) {
   const SolveDev& s = c->sd;
-  cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st);
-  c->D->e1(s, c->L[0], c->st, last ? 1 : 0, 0, -1);
+  c->D->e1(s, c->L[0], c->st, last ? 1 : 0, 0, -1);  // also zeroes the stage's wave speed
   c->D->f1(s, c->st);
   c->D->e2(s, c->L[1], c->st);  // also the face AV viscosities
   c->D->e3(s, rk, c->L[2], c->st);  // averages the grad Q traces where it reads them
@@ -705,7 +704,6 @@ void enqueue_step_host(ChorusCtx* c, bool diag, const double* Qin, double* Qout)
   auto cut = [&](int i) { return (int)((long long)NC * i / K); };
   RKStage r[5];
   make_rk(c, diag, r);
-  cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st);
   if (Qin) {
     cudaEventRecord(c->ev[2 * kHostChunks], c->st);  // earlier work on the state is done
     cudaStreamWaitEvent(c->cp, c->ev[2 * kHostChunks], 0);

@@ -31,6 +31,10 @@ namespace chorus {
 constexpr int kHalfF = kMaxN / 2 + 1;  // flux points up to the middle of a line
 constexpr int kHalfS = kMaxN / 2;      // mirrored pairs of solution points
 
+// wait for the predecessor grid of a programmatic (PDL) launch: its completion and its
+// memory; a no-op for a launch without the attribute
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 struct OpsN {
   double L[(kMaxN + 1) * kMaxN];  // Lmat(N+1,N) column-major
   double M[(kMaxN + 1) * kMaxN];  // Mmat(N+1,N)
@@ -301,6 +305,10 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
 template <int N>
 __global__ void __launch_bounds__(512) k_e1(SolveDev s, int epb, int sensor, int c0, int c1) {
   extern __shared__ double sm[];
+  pdl_wait();
+  // bit 4: the first pass of a stage, which starts the stage's wave-speed maximum
+  if ((sensor & 4) && c0 == 0 && blockIdx.x == 0 && threadIdx.x == 0) *s.eig = 0ull;
+  sensor &= 3;
   const int e0 = c0 + blockIdx.x * epb;
   const int cnt = min(epb, c1 - e0);
   if (cnt <= 0) return;
@@ -406,6 +414,7 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
 
 template <int N>
 __global__ void __launch_bounds__(256) k_f1(SolveDev s) {
+  pdl_wait();
   const unsigned long long evb = f1_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
   block_max_ull(evb, s.eig);
 }
@@ -532,6 +541,7 @@ __device__ __forceinline__ bool needs_gradients(const SolveDev& s, int c) {
 template <int N>
 __global__ void __launch_bounds__(512) k_e2(SolveDev s, int epb, int chunk) {
   extern __shared__ double sm[];
+  pdl_wait();
   __shared__ int list[512];
   __shared__ int woff[17];
   const int c0 = blockIdx.x * chunk;
@@ -751,6 +761,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
 template <int N>
 __global__ void __launch_bounds__(512) k_e3(SolveDev s, RKStage rk, int epb, int update) {
   extern __shared__ double sm[];
+  pdl_wait();
   const int e0 = blockIdx.x * epb;
   const int cnt = min(epb, s.NC - e0);
   if (cnt <= 0) return;
@@ -841,6 +852,7 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
 template <int N>
 __global__ void __launch_bounds__(256) k_ct_elem(SolveDev s, int epb, int mode, int c0, int c1) {
   extern __shared__ double sm[];
+  pdl_wait();
   const int e0 = c0 + blockIdx.x * epb;
   const int cnt = min(epb, c1 - e0);
   if (cnt <= 0) return;
@@ -864,6 +876,7 @@ __device__ __forceinline__ void ctface_point(const SolveDev& s, int t) {
 
 template <int N>
 __global__ void __launch_bounds__(256) k_ct_face(SolveDev s) {
+  pdl_wait();
   ctface_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
 }
 

@@ -23,6 +23,25 @@ inline size_t smem_e3(int epb) {
 }
 inline size_t smem_ct(int epb) { return sizeof(double) * epb * D<kN>::NFP * 2; }
 inline int grid_cells(int nc, int epb) { return (nc + epb - 1) / epb; }
+
+// Launch with programmatic stream serialization: the kernel may be scheduled while its
+// predecessor on the stream drains, and waits (griddepcontrol.wait, at its entry) for
+// the predecessor's completion and memory before touching any of its data.  Hides the
+// launch gap between dependent passes; the wait is hardware-managed.
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
 // threads per CTA of a face-point pass: 256, or 64 when that leaves fewer than about
 // eight CTAs per SM (small meshes), so that the points spread over every SM
 inline int face_threads(int n) { return n >= 152 * 8 * 256 ? 256 : 64; }
@@ -48,17 +67,17 @@ void CHORUS_CAT(upload_ops_n, CHORUS_N)(const OpsN& o) {
 
 template <>
 void launch_e1<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int plot, int c0, int c1) {
-  const int sensor = s.artiv ? (plot ? 3 : 1) : 0;
+  const int sensor = (s.artiv ? (plot ? 3 : 1) : 0) | 4;  // 4: also reset the stage's wave speed
   if (c1 < 0) c1 = s.NC;
-  if (c1 > c0) k_e1<kN><<<grid_cells(c1 - c0, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, sensor, c0, c1);
+  if (c1 > c0) launch_pdl(k_e1<kN>, grid_cells(c1 - c0, L.epb), L.threads, smem_e1(L.epb), st, s, L.epb, sensor, c0, c1);
 }
 void CHORUS_CAT(launch_e1_nosensor_n, CHORUS_N)(const SolveDev& s, const Launch& L, cudaStream_t st) {
-  k_e1<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st>>>(s, L.epb, 0, 0, s.NC);
+  launch_pdl(k_e1<kN>, grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st, s, L.epb, 0, 0, s.NC);
 }
 template <>
 void launch_f1<kN>(const SolveDev& s, cudaStream_t st) {
   const int n = (s.nface2 + s.nface1) * kN;
-  if (n > 0) k_f1<kN><<<(n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st>>>(s);
+  if (n > 0) launch_pdl(k_f1<kN>, (n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st, s);
 }
 template <>
 void launch_e2<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
@@ -76,7 +95,7 @@ void launch_e2<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
   chunk = chunk < L.epb ? L.epb : (chunk > L.threads ? L.threads : chunk);
   chunk -= chunk % L.epb;
   if (!s.skip) chunk = L.epb;  // every cell needs its gradients: one group per CTA
-  k_e2<kN><<<grid_cells(s.NC, chunk), L.threads, smem_e2(L.epb), st>>>(s, L.epb, chunk);
+  launch_pdl(k_e2<kN>, grid_cells(s.NC, chunk), L.threads, smem_e2(L.epb), st, s, L.epb, chunk);
 }
 template <>
 void launch_f2<kN>(const SolveDev& s, cudaStream_t st) {
@@ -86,16 +105,17 @@ void launch_f2<kN>(const SolveDev& s, cudaStream_t st) {
 template <>
 void launch_e3<kN>(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st) {
   const int update = (rk.cQ != 0.0 || rk.cR != 0.0 || rk.nsrc > 0) ? 1 : 0;
-  k_e3<kN><<<grid_cells(s.NC, L.epb), L.threads, smem_e3(L.epb), st>>>(s, rk, L.epb, update);
+  launch_pdl(k_e3<kN>, grid_cells(s.NC, L.epb), L.threads, smem_e3(L.epb), st, s, rk, L.epb, update);
 }
 template <>
 void launch_ct<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int mode, int c0, int c1) {
   if (mode == 1) {
     const int n = s.nface2 * kN;
-    if (n > 0) k_ct_face<kN><<<(n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st>>>(s);
+    if (n > 0) launch_pdl(k_ct_face<kN>, (n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st, s);
   } else {
     if (c1 < 0) c1 = s.NC;
-    if (c1 > c0) k_ct_elem<kN><<<grid_cells(c1 - c0, L.epb), L.threads, smem_ct(L.epb), st>>>(s, L.epb, mode, c0, c1);
+    if (c1 > c0)
+      launch_pdl(k_ct_elem<kN>, grid_cells(c1 - c0, L.epb), L.threads, smem_ct(L.epb), st, s, L.epb, mode, c0, c1);
   }
 }
 template <>
