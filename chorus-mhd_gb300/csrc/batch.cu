@@ -103,7 +103,9 @@ __device__ __forceinline__ void for_each_tile(int* counter, int nt, const int4* 
 // each cell pass walks its own tile list, cut with that pass's cells per CTA
 __global__ void __launch_bounds__(256) kb_e1(BatchDev b, int slot, int sensor_on) {
   extern __shared__ double sm[];
+  pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[0], b.ctiles, b.solves, [&](const int4& T, const SolveDev& s) {
+    if (T.y == 0 && threadIdx.x == 0) *s.eig = 0ull;  // the solve's stage starts its wave-speed maximum
     // 1: variable-1 sensor; 3: also variable 6 when the solve's plot flag is set
     const int sensor = s.artiv ? ((sensor_on & 2) && !*s.plot_flag ? 1 : sensor_on) : 0;
 #define CALL(n) e1_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sensor, sm)
@@ -114,6 +116,7 @@ __global__ void __launch_bounds__(256) kb_e1(BatchDev b, int slot, int sensor_on
 
 __global__ void __launch_bounds__(256) kb_e2(BatchDev b, int slot) {
   extern __shared__ double sm[];
+  pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[2], b.ctiles + b.ntiles[0], b.solves,
                 [&](const int4& T, const SolveDev& s) {
 #define CALL(n) e2_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sm)
@@ -124,6 +127,7 @@ __global__ void __launch_bounds__(256) kb_e2(BatchDev b, int slot) {
 
 __global__ void __launch_bounds__(128) kb_e3(BatchDev b, int slot, int stage) {
   extern __shared__ double sm[];
+  pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[3], b.ctiles + b.ntiles[0] + b.ntiles[2], b.solves,
                 [&](const int4& T, const SolveDev& s) {
                   const RKStage& rk = b.rk[stage * b.cap + T.x];
@@ -135,6 +139,7 @@ __global__ void __launch_bounds__(128) kb_e3(BatchDev b, int slot, int stage) {
 
 __global__ void __launch_bounds__(128) kb_ct(BatchDev b, int slot, int mode) {
   extern __shared__ double sm[];
+  pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[4], b.ctiles + b.ntiles[0] + b.ntiles[2] + b.ntiles[3], b.solves,
                 [&](const int4& T, const SolveDev& s) {
 #define CALL(n) ct_elem_body<n, OpsAll<n>>(s, T.y, T.z, T.z, mode, sm)
@@ -145,6 +150,7 @@ __global__ void __launch_bounds__(128) kb_ct(BatchDev b, int slot, int mode) {
 
 // face passes: which = 0 Rusanov (F1), 1 grad Q trace averages (not part of a step), 2 CT average
 __global__ void __launch_bounds__(128) kb_face(BatchDev b, int slot, int which) {
+  pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[1], b.ftiles, b.solves, [&](const int4& T, const SolveDev& s) {
     // a tile holds 128 to kFaceTileMax points, taken blockDim.x at a time
     unsigned long long evb = 0ull;
@@ -240,7 +246,7 @@ struct ChorusBatch {
   int ctiles = 0, ftiles = 0;
 };
 
-static constexpr int kCounterSlots = 16;
+static constexpr int kCounterSlots = 32;  // one tile counter per launch of a step (5 x 4 + 3)
 static constexpr int kFaceTileMax = 1024;  // face points per tile of the face passes, at most
 
 static int batch_alloc(ChorusBatch* b, int cap_solves, int cap_ctiles, int cap_ftiles) {
@@ -378,18 +384,20 @@ static void batch_enqueue_step(ChorusBatch* b) {
   a.cap = b->cap_solves;
   a.pad = 0;
   const size_t* sm = b->smem;
-  for (int stage = 0; stage < 5; stage++) {
-    cudaMemsetAsync(b->d_counters, 0, sizeof(int) * kCounterSlots, b->st);
-    cudaMemsetAsync(b->d_eig, 0, sizeof(unsigned long long) * 2 * b->cap_solves, b->st);
-    kb_e1<<<b->grid_cells, 256, sm[0], b->st>>>(a, 0, stage == 4 ? 3 : 1);
-    kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 1, 0);
-    kb_e2<<<b->grid_cells, 256, sm[1], b->st>>>(a, 2);  // also the face AV viscosities
-    kb_e3<<<b->grid_cells, 128, sm[2], b->st>>>(a, 4, stage);
-  }
+  // every launch of the step has its own tile counter, so one memset per step clears
+  // them all; E1 starts each solve's wave-speed maximum; the launches are programmatic
+  // (each is scheduled while its predecessor drains and waits for it at entry)
   cudaMemsetAsync(b->d_counters, 0, sizeof(int) * kCounterSlots, b->st);
-  kb_ct<<<b->grid_cells, 128, sm[3], b->st>>>(a, 5, 0);
-  kb_face<<<b->grid_faces, 128, 0, b->st>>>(a, 6, 2);
-  kb_ct<<<b->grid_cells, 128, sm[3], b->st>>>(a, 7, 2);
+  for (int stage = 0; stage < 5; stage++) {
+    const int c0 = 4 * stage;
+    launch_pdl(kb_e1, b->grid_cells, 256, sm[0], b->st, a, c0, stage == 4 ? 3 : 1);
+    launch_pdl(kb_face, b->grid_faces, 128, 0, b->st, a, c0 + 1, 0);
+    launch_pdl(kb_e2, b->grid_cells, 256, sm[1], b->st, a, c0 + 2);  // also the face AV viscosities
+    launch_pdl(kb_e3, b->grid_cells, 128, sm[2], b->st, a, c0 + 3, stage);
+  }
+  launch_pdl(kb_ct, b->grid_cells, 128, sm[3], b->st, a, 20, 0);
+  launch_pdl(kb_face, b->grid_faces, 128, 0, b->st, a, 21, 2);
+  launch_pdl(kb_ct, b->grid_cells, 128, sm[3], b->st, a, 22, 2);
 }
 
 extern "C" {

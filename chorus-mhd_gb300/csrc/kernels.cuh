@@ -35,6 +35,26 @@ constexpr int kHalfS = kMaxN / 2;      // mirrored pairs of solution points
 // memory; a no-op for a launch without the attribute
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// Launch with programmatic stream serialization: the kernel may be scheduled while its
+// predecessor on the stream drains, and waits (griddepcontrol.wait, at its entry) for
+// the predecessor's completion and memory before touching any of its data.  Hides the
+// launch gap between dependent passes; the wait is hardware-managed.
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
+
 struct OpsN {
   double L[(kMaxN + 1) * kMaxN];  // Lmat(N+1,N) column-major
   double M[(kMaxN + 1) * kMaxN];  // Mmat(N+1,N)

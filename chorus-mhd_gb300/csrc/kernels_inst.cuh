@@ -24,24 +24,6 @@ inline size_t smem_e3(int epb) {
 inline size_t smem_ct(int epb) { return sizeof(double) * epb * D<kN>::NFP * 2; }
 inline int grid_cells(int nc, int epb) { return (nc + epb - 1) / epb; }
 
-// Launch with programmatic stream serialization: the kernel may be scheduled while its
-// predecessor on the stream drains, and waits (griddepcontrol.wait, at its entry) for
-// the predecessor's completion and memory before touching any of its data.  Hides the
-// launch gap between dependent passes; the wait is hardware-managed.
-template <typename... KArgs, typename... Args>
-inline void launch_pdl(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
-}
 // threads per CTA of a face-point pass: 256, or 64 when that leaves fewer than about
 // eight CTAs per SM (small meshes), so that the points spread over every SM
 inline int face_threads(int n) { return n >= 152 * 8 * 256 ? 256 : 64; }
@@ -56,6 +38,7 @@ void set_smem_limits() {
   cudaFuncSetAttribute(k_e2<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   cudaFuncSetAttribute(k_e3<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   cudaFuncSetAttribute(k_ct_elem<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(k_diag_interp<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (dev < 64) done[dev] = true;
 }
 }  // namespace
