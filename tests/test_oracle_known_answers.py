@@ -64,6 +64,30 @@ def test_free_stream_preservation(case_root, N):
     assert np.abs(r).max() < 1e-11
 
 
+@pytest.mark.parametrize("N,jitter", [(3, 0.0), (5, 0.1)])
+def test_periodic_totals_are_conserved(case_root, N, jitter):
+    """The common face fluxes are single-valued and the residual is the derivative of a
+    degree-N flux polynomial, so over a periodic domain the totals sum(Jac w_i w_j Q_v)
+    (w the interpolatory weights of the solution points) of the eight conserved
+    variables change by round-off only."""
+    o = oracle.Oracle(make_case(case_root, problem="orszag_tang", nx=6, ny=5, N=N, jitter=jitter, seed=2))
+    xs = o.array("Xs")
+    w = np.linalg.solve(np.vander(xs, N, increasing=True).T, 1.0 / np.arange(1, N + 1))
+    J = o.array("Jac")
+    wJ = J * np.tile(np.outer(w, w).ravel(), J.size // (N * N))
+
+    def totals():
+        Q = o.array("Q").reshape(-1, 9)
+        return (Q * wJ[:, None]).sum(0), (np.abs(Q) * wJ[:, None]).sum(0)
+
+    t0, scale = totals()
+    o.run(20)
+    t1, _ = totals()
+    ref = max(scale[0], scale[4])
+    assert np.all(np.abs(t1[:8] - t0[:8]) <= 1e-13 * ref)
+    assert abs(t1[8] - t0[8]) > 1e-9 * ref  # A_z is advected in non-conservative form
+
+
 def test_ct_keeps_divb_at_roundoff_on_affine_mesh(case_root):
     o = oracle.Oracle(make_case(case_root, problem="orszag_tang", nx=8, ny=8, N=4, steps=1))
     res, divb = o.step()
