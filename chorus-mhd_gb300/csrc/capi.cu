@@ -71,6 +71,9 @@ static void make_ops(int N, const double* Lmat, const double* Mmat, const double
     }
     o.LMID[f] = (N & 1) ? Lmat[f + (N + 1) * ((N - 1) / 2)] : 0.0;
   }
+  o.LS = fix_shift_for(Lmat, (N + 1) * N);
+  for (int f = 0; f <= N; f++)
+    for (int j = 0; j < N; j++) fix_split_coef(Lmat[f + (N + 1) * j], o.LS, &o.LH[f * N + j], &o.LL[f * N + j]);
   // AV smoothing A = Hlow * H: project N points onto the N-1 low-order points
   // (hhval at Xs_low, AV.f90:19-35) and evaluate back (hhval_low at Xs, :41-58)
   double xsl[kMaxN], xfl[kMaxN + 1];

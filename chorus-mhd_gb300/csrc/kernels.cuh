@@ -24,6 +24,7 @@
 #include <cstdint>
 
 #include "chorus_internal.h"
+#include "fixdot.cuh"
 #include "physics.cuh"
 
 namespace chorus {
@@ -70,6 +71,10 @@ struct OpsN {
   double CE[kHalfF * kHalfS];
   double CO[kHalfF * kHalfS];
   double LMID[kHalfF];
+  // the integer form of Lmat (fixdot.cuh): LH/LL[f*N + j] = limbs of round(L(f,j) 2^LS)
+  int LH[(kMaxN + 1) * kMaxN];
+  int LL[(kMaxN + 1) * kMaxN];
+  int LS;
 };
 
 // one copy per translation unit; upload_ops_n<N>() fills it
@@ -190,8 +195,10 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
   }
   __syncthreads();
   // interpolation to every flux point, one (cell, line, variable) per thread so that
-  // every lane of every warp does FP64 work; the mirror symmetry of the points halves
-  // the multiplications (see OpsN::CE)
+  // every lane of every warp does work.  The line operator runs on the integer pipes
+  // (fixdot.cuh), which the FP64 work of the pass leaves idle; lines with non-finite or
+  // huge values keep the FP64 form, where the mirror symmetry of the points halves the
+  // multiplications (see OpsN::CE)
   for (int t = threadIdx.x; t < cnt * 2 * N * 9; t += blockDim.x) {
     const int k = t % 9, el = t / 9, e = el / (2 * N), line = el - e * 2 * N;
     const double* q = sQ + e * NS * 9 + k;
@@ -205,6 +212,15 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
     double v[N];
 #pragma unroll
     for (int sp = 0; sp < N; sp++) v[sp] = qb[sp * qs];
+    const int emax = fix_emax(v);
+    if (emax <= kFixEmaxFast) {
+      int h[N], l[N];
+      fix_align(v, emax, h, l);
+      const int sc = emax - 1017 - kFixG - O::ops().LS;
+#pragma unroll
+      for (int f = 0; f <= N; f++) ob[f * os] = fix_dot(h, l, O::ops().LH + f * N, O::ops().LL + f * N, sc);
+      continue;
+    }
     double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
 #pragma unroll
     for (int j = 0; j < N / 2; j++) {
