@@ -74,6 +74,8 @@ static void make_ops(int N, const double* Lmat, const double* Mmat, const double
   o.LS = fix_shift_for(Lmat, (N + 1) * N);
   for (int f = 0; f <= N; f++)
     for (int j = 0; j < N; j++) fix_split_coef(Lmat[f + (N + 1) * j], o.LS, &o.LH[f * N + j], &o.LL[f * N + j]);
+  o.MS = fix_shift_for(Mmat, (N + 1) * N);
+  for (int i = 0; i < (N + 1) * N; i++) fix_split_coef(Mmat[i], o.MS, &o.MH[i], &o.ML[i]);
   // AV smoothing A = Hlow * H: project N points onto the N-1 low-order points
   // (hhval at Xs_low, AV.f90:19-35) and evaluate back (hhval_low at Xs, :41-58)
   double xsl[kMaxN], xfl[kMaxN + 1];

@@ -75,6 +75,11 @@ struct OpsN {
   int LH[(kMaxN + 1) * kMaxN];
   int LL[(kMaxN + 1) * kMaxN];
   int LS;
+  // and of Mmat: MH/ML[i*(N+1) + r] = limbs of round(M(r,i) 2^MS), the weight of flux
+  // point r in the derivative at solution point i (the column-major index of Mmat)
+  int MH[(kMaxN + 1) * kMaxN];
+  int ML[(kMaxN + 1) * kMaxN];
+  int MS;
 };
 
 // one copy per translation unit; upload_ops_n<N>() fills it
@@ -184,13 +189,11 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
   double* sT = sQ + epb * NS * 9;     // [epb][NS]      sensor scratch
   double* sU = sT + epb * NS;         // [epb][NS]
   double* sV = sU + epb * NS;         // [epb][NFP][9]  flux-point values
-  double* sL = sV + epb * NFP * 9;    // Lmat (N+1, N)
-  double* sA = sL + (N + 1) * N;      // AV smoothing operator (N, N)
+  double* sA = sV + epb * NFP * 9;    // AV smoothing operator (N, N)
   {
     // all global traffic of the pass is contiguous block copies (coalesced)
     const double* g = s.Q + (size_t)e0 * NS * 9;
     for (int i = threadIdx.x; i < cnt * NS * 9; i += blockDim.x) sQ[i] = g[i];
-    for (int i = threadIdx.x; i < (N + 1) * N; i += blockDim.x) sL[i] = O::ops().L[i];
     for (int i = threadIdx.x; i < N * N; i += blockDim.x) sA[i] = O::ops().A[i];
   }
   __syncthreads();
@@ -631,6 +634,32 @@ __global__ void __launch_bounds__(256) k_f2(SolveDev s) {
   f2_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// the derivative along one line, y_i = sum_r M(r,i) x_r (i < N) from the N+1 flux values
+// x_r = x[r*xs]: the integer form (fixdot.cuh), or FP64 for a line with non-finite or
+// huge values
+template <int N, class O>
+__device__ __forceinline__ void deriv_line(const double* x, int xs, double (&y)[N]) {
+  double v[N + 1];
+#pragma unroll
+  for (int r = 0; r <= N; r++) v[r] = x[r * xs];
+  const int emax = fix_emax(v);
+  if (emax <= kFixEmaxFast) {
+    int h[N + 1], l[N + 1];
+    fix_align(v, emax, h, l);
+    const int sc = emax - 1017 - kFixG - O::ops().MS;
+#pragma unroll
+    for (int i = 0; i < N; i++) y[i] = fix_dot(h, l, O::ops().MH + i * (N + 1), O::ops().ML + i * (N + 1), sc);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      double a = 0.0;
+#pragma unroll
+      for (int r = 0; r <= N; r++) a += O::ops().M[r + (N + 1) * i] * v[r];
+      y[i] = a;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // E3: viscous + AV flux, divergence, A_z advection, RK update
 // ---------------------------------------------------------------------------
@@ -644,7 +673,6 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
   double* sJ = sR + epb * NS * 9;   // [epb][NS] 1/J
   double* sZ = sJ + epb * NS;       // [epb][NFP][2] A_z * (S_x, S_y) at the flux points
   double* sN = sZ + epb * NFP * 2;  // [epb][NS][2] grad A_z
-  double* sM = sN + epb * NS * 2;   // Mmat (N+1, N)
   __shared__ int list[64];
   const int nact = active_cells(s, e0, cnt, 1, list);
   {
@@ -661,7 +689,6 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
       sZ[2 * i] = z * s.met[2 * g];
       sZ[2 * i + 1] = z * s.met[2 * g + 1];
     }
-    for (int i = threadIdx.x; i < (N + 1) * N; i += blockDim.x) sM[i] = O::ops().M[i];
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nact * NFP; t += blockDim.x) {
@@ -715,37 +742,41 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
     }
   }
   __syncthreads();
-  // divergence of the total flux, one (cell, point, variable) per thread, then grad
-  // A_z in the conservative form of nablaAsp (magnetic_potential.f90:1-42),
-  // (1/J) sum_r Mmat (A_z S) over both line families, one (cell, point, component) per
-  // thread; 2(N+1) FMAs per item either way, and the two ranges split between warps
-  // (only the warp that straddles them diverges)
-  const int ndiv = cnt * NS * 8;
-  for (int t = threadIdx.x; t < ndiv + cnt * NS * 2; t += blockDim.x) {
-    double a = 0.0;
-    if (t < ndiv) {
-      const int k = t & 7, ep = t >> 3, e = ep / NS, p = ep - e * NS, is = p % N, js = p / N;
-      const double* Fe = sF + e * NFP * 8 + k;
+  // divergence of the total flux and grad A_z in the conservative form of nablaAsp
+  // (magnetic_potential.f90:1-42), (1/J) sum_r Mmat (A_z S): ten line quantities per
+  // cell (eight flux components, two A_z S components), each differentiated along its
+  // lines on the integer pipes, one (cell, line, quantity) per thread; first the
+  // family-1 lines (xi), then the family-2 lines (eta), which add to them and scale by
+  // 1/J
+  constexpr int NQ = 10;
+#pragma unroll 1
+  for (int fam = 0; fam < 2; fam++) {
+    for (int t = threadIdx.x; t < cnt * N * NQ; t += blockDim.x) {
+      const int k = t % NQ, el = t / NQ, e = el / N, ln = el - e * N;
+      const bool fl = k < 8;
+      // flux point r of line ln: family 1 at ln*(N+1) + r, family 2 at NF1 + r*N + ln
+      const int fp0 = fam ? NF1 + ln : ln * (N + 1), fps = fam ? N : 1;
+      const double* x = fl ? sF + (e * NFP + fp0) * 8 + k : sZ + (e * NFP + fp0) * 2 + (k - 8);
+      double y[N];
+      deriv_line<N, O>(x, fl ? fps * 8 : fps * 2, y);
+      // solution point i of line ln: family 1 at ln*N + i, family 2 at i*N + ln
+      const int p0 = e * NS + (fam ? ln : ln * N), ps = fam ? N : 1;
+      double* out = fl ? sR + p0 * 9 + k : sN + p0 * 2 + (k - 8);
+      const int os = fl ? ps * 9 : ps * 2;
+      if (!fam) {
 #pragma unroll
-      for (int r = 0; r <= N; r++) {
-        a += sM[r + (N + 1) * is] * Fe[(js * (N + 1) + r) * 8];
-        a += sM[r + (N + 1) * js] * Fe[(NF1 + r * N + is) * 8];
-      }
-      sR[ep * 9 + k] = a * sJ[ep];
-    } else {
-      const int u = t - ndiv, c = u & 1, ep = u >> 1, e = ep / NS, p = ep - e * NS, is = p % N, js = p / N;
-      const double* az = sZ + e * NFP * 2 + c;
+        for (int i = 0; i < N; i++) out[i * os] = y[i];
+      } else {
 #pragma unroll
-      for (int r = 0; r <= N; r++) {
-        a += sM[r + (N + 1) * is] * az[(js * (N + 1) + r) * 2];
-        a += sM[r + (N + 1) * js] * az[(NF1 + r * N + is) * 2];
+        for (int i = 0; i < N; i++) {
+          const double a = (out[i * os] + y[i]) * sJ[p0 + i * ps];
+          out[i * os] = a;
+          if (!fl) s.nAs[((size_t)e0 * NS + p0 + i * ps) * 2 + (k - 8)] = a;
+        }
       }
-      a *= sJ[ep];
-      sN[u] = a;
-      s.nAs[(size_t)e0 * NS * 2 + u] = a;
     }
+    __syncthreads();
   }
-  __syncthreads();
   // A_z advection (resid(9), compresid.f90:45-47) at every solution point
   for (int t = threadIdx.x; t < cnt * NS; t += blockDim.x) {
     const double* q = s.Q + ((size_t)e0 * NS + t) * 9;

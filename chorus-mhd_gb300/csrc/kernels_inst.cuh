@@ -13,13 +13,13 @@ namespace chorus {
 namespace {
 constexpr int kN = CHORUS_N;
 inline size_t smem_e1(int epb) {
-  return sizeof(double) * ((size_t)epb * (D<kN>::NS * 9 + 2 * D<kN>::NS + D<kN>::NFP * 9) + (kN + 1) * kN + kN * kN);
+  return sizeof(double) * ((size_t)epb * (D<kN>::NS * 9 + 2 * D<kN>::NS + D<kN>::NFP * 9) + kN * kN);
 }
 inline size_t smem_e2(int epb) {
   return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 9 + D<kN>::NG * D<kN>::NS + D<kN>::NS * 16));
 }
 inline size_t smem_e3(int epb) {
-  return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 8 + D<kN>::NS * (1 + 9 + 1 + 2) + D<kN>::NFP * 2) + (kN + 1) * kN);
+  return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 8 + D<kN>::NS * (1 + 9 + 1 + 2) + D<kN>::NFP * 2));
 }
 inline size_t smem_ct(int epb) { return sizeof(double) * epb * D<kN>::NFP * 2; }
 inline int grid_cells(int nc, int epb) { return (nc + epb - 1) / epb; }
