@@ -269,35 +269,6 @@ static int batch_alloc(ChorusBatch* b, int cap_solves, int cap_ctiles, int cap_f
   return CHORUS_OK;
 }
 
-// RK stage records of one solve (same coefficients as the single-solve path)
-static void rk_records(const SolveDev& s, double dt, int k_stage, RKStage* r) {
-  for (int k = 0; k < 5; k++) std::memset(&r[k], 0, sizeof(RKStage));
-  if (k_stage == 5) {
-    const double a11 = 0.39175222700392, a21 = 0.44437049406734, a22 = 0.55562950593266, a23 = 0.36841059262959,
-                 a31 = 0.6201018513854, a32 = 0.3798981486146, a33 = 0.25189177424738, a41 = 0.17807995410773,
-                 a42 = 0.82192004589227, a43 = 0.54497475021237, a51 = 0.00683325884039, a52 = 0.51723167208978,
-                 a53 = 0.12759831133288, a54 = 0.34833675773694, a55 = 0.08460416338212, a56 = 0.22600748319395;
-    r[0].cQ = 1.0; r[0].cR = dt * a11; r[0].save_old = s.Qk0;
-    r[1].nsrc = 1; r[1].src[0] = s.Qk0; r[1].c[0] = a21; r[1].cQ = a22; r[1].cR = a23 * dt; r[1].save_new = s.Qr2;
-    r[2].nsrc = 1; r[2].src[0] = s.Qk0; r[2].c[0] = a31; r[2].cQ = a32; r[2].cR = a33 * dt; r[2].save_new = s.Qr3;
-    r[3].nsrc = 1; r[3].src[0] = s.Qk0; r[3].c[0] = a41; r[3].cQ = a42; r[3].cR = a43 * dt; r[3].save_R = s.R0;
-    r[4].nsrc = 3; r[4].src[0] = s.Qk0; r[4].src[1] = s.Qr2; r[4].src[2] = s.Qr3;
-    r[4].c[0] = a51; r[4].c[1] = a52; r[4].c[2] = a53; r[4].cQ = a54; r[4].cR = a56 * dt;
-    r[4].R0 = s.R0; r[4].cR0 = a55 * dt;
-  } else {
-    const double a30 = 0.355909775063327, a32 = 0.644090224936674, a40 = 0.367933791638137,
-                 a43 = 0.632066208361863, a52 = 0.237593836598569, a54 = 0.762406163401431,
-                 b10 = 0.377268915331368, b21 = 0.377268915331368, b32 = 0.242995220537396,
-                 b43 = 0.238458932846290, b54 = 0.287632146308408;
-    r[0].cQ = 1.0; r[0].cR = b10 * dt; r[0].save_old = s.Qk0;
-    r[1].cQ = 1.0; r[1].cR = b21 * dt; r[1].save_new = s.Qka;
-    r[2].nsrc = 1; r[2].src[0] = s.Qk0; r[2].c[0] = a30; r[2].cQ = a32; r[2].cR = b32 * dt;
-    r[3].nsrc = 1; r[3].src[0] = s.Qk0; r[3].c[0] = a40; r[3].cQ = a43; r[3].cR = b43 * dt;
-    r[4].nsrc = 1; r[4].src[0] = s.Qka; r[4].c[0] = a52; r[4].cQ = a54; r[4].cR = b54 * dt;
-  }
-  r[4].write_resid = 1;
-}
-
 static int batch_rebuild(ChorusBatch* b) {
   std::vector<int> act;
   for (int i = 0; i < (int)b->slots.size(); i++)
@@ -343,7 +314,7 @@ static int batch_rebuild(ChorusBatch* b) {
     sd[i].eig = b->d_eig + 2 * i;
     sd[i].err = b->d_err + i;
     RKStage r[5];
-    rk_records(sd[i], b->slots[i].dt, b->slots[i].k_stage, r);
+    rk_stage_records(sd[i], b->slots[i].dt, b->slots[i].k_stage, false, r);
     for (int k = 0; k < 5; k++) rk[(size_t)k * b->cap_solves + i] = r[k];
   }
   cudaError_t e = cudaSuccess;

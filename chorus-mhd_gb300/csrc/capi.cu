@@ -639,13 +639,13 @@ RKStage rk_blank() {
   return r;
 }
 
+}  // namespace
+
 // the records of the five stages of RK_S5P3 (iterations.f90:162-217) or FiveStageRk
-// (:92-160); `diag` marks the last stage to accumulate the residual norm
-void make_rk(ChorusCtx* c, bool diag, RKStage* r) {
-  const SolveDev& s = c->sd;
-  const double dt = c->p.dt;
-  for (int k = 0; k < 5; k++) r[k] = rk_blank();
-  if (c->p.k_stage == 5) {
+// (:92-160) of one solve; `diag` marks the last stage to accumulate the residual norm
+void chorus::rk_stage_records(const SolveDev& s, double dt, int k_stage, bool diag, RKStage* r) {
+  for (int k = 0; k < 5; k++) std::memset(&r[k], 0, sizeof(RKStage));
+  if (k_stage == 5) {
     const double a11 = 0.39175222700392, a21 = 0.44437049406734, a22 = 0.55562950593266, a23 = 0.36841059262959,
                  a31 = 0.6201018513854, a32 = 0.3798981486146, a33 = 0.25189177424738, a41 = 0.17807995410773,
                  a42 = 0.82192004589227, a43 = 0.54497475021237, a51 = 0.00683325884039, a52 = 0.51723167208978,
@@ -671,6 +671,10 @@ void make_rk(ChorusCtx* c, bool diag, RKStage* r) {
   r[4].diag = diag ? 1 : 0;
   r[4].write_resid = 1;  // the last stage's residual stays available like the reference's resid
 }
+
+namespace {
+
+void make_rk(ChorusCtx* c, bool diag, RKStage* r) { rk_stage_records(c->sd, c->p.dt, c->p.k_stage, diag, r); }
 
 void enqueue_rk(ChorusCtx* c, bool diag) {
   RKStage r[5];

@@ -114,6 +114,9 @@ struct RKStage {
   int diag;         // accumulate sum(resid^2) per cell into diag[e][0]
 };
 
+// the five stage records of RK_S5P3 / FiveStageRk for one solve (capi.cu)
+void rk_stage_records(const SolveDev& s, double dt, int k_stage, bool diag, RKStage* r);
+
 // launch helpers implemented in kernels_*.cu (one translation unit per N)
 struct Launch {
   int epb;    // cells per CTA in element kernels

@@ -8,7 +8,7 @@
 //   * the inputs of one line are aligned to the largest exponent among them and held as
 //     57-bit signed integers X_j = x_j * 2^(1075 + G - emax) (G = 4 guard bits below the
 //     53-bit significand of the largest input; smaller inputs lose only bits below
-//     2^-57 of the largest),
+//     2^-58 of the largest, by rounding),
 //   * the coefficients as 59-bit signed integers c = round(C * 2^S), S per operator,
 //   * both split at bit 29 (X = h 2^29 + l, c = ch 2^29 + cl, 0 <= l, cl < 2^29), so the
 //     product sum is four 32x32->64 multiply-adds per term, exact in three 64-bit
@@ -79,8 +79,8 @@ FIX_HD int fix_emax(const double (&v)[NI]) {
   return e;
 }
 
-// aligned limbs of a line: X_j = h_j 2^29 + l_j = x_j 2^(1075 + G - emax), truncated
-// toward zero in magnitude
+// aligned limbs of a line: X_j = h_j 2^29 + l_j = x_j 2^(1075 + G - emax), rounded to
+// the nearest integer (ties away from zero in magnitude)
 template <int NI>
 FIX_HD void fix_align(const double (&v)[NI], int emax, int (&h)[NI], int (&l)[NI]) {
 #pragma unroll
@@ -90,7 +90,7 @@ FIX_HD void fix_align(const double (&v)[NI], int emax, int (&h)[NI], int (&l)[NI
     int d = emax - (e ? e : 1);  // zeros and subnormals have exponent 1, no hidden bit
     d = d < 63 ? d : 63;         // inputs 2^-59 below the largest vanish
     const uint64_t m = ((u & 0xfffffffffffffull) | (e ? 0x10000000000000ull : 0ull)) << kFixG;
-    int64_t x = (int64_t)(m >> d);
+    int64_t x = (int64_t)((m + ((1ull << d) >> 1)) >> d);  // rounded to the nearest unit
     x = (u >> 63) ? -x : x;
     h[j] = (int)(x >> kFixSplit);
     l[j] = (int)(x & ((1 << kFixSplit) - 1));
@@ -124,13 +124,14 @@ FIX_HD double fix_dot(const int (&h)[NI], const int (&l)[NI], const int* ch, con
   return fix_double(sgn | (((uint64_t)(E - 1) << 52) + mant));
 }
 
-// integer form of a coefficient matrix (host side): c = round(C 2^S), S the largest
-// shift that keeps every |c| below 2^59
+// integer form of coefficients (host side): c = round(C 2^S), S the largest shift that
+// keeps every |c| below 2^59 (S = 59 - e for max |C| in [2^(e-1), 2^e))
 inline int fix_shift_for(const double* C, int n) {
   double mx = 0.0;
   for (int i = 0; i < n; i++) mx = C[i] > mx ? C[i] : (-C[i] > mx ? -C[i] : mx);
-  int e = 0;  // smallest e with max |C| < 2^e
-  while ((double)(1ull << e) <= mx && e < 30) e++;
+  if (mx == 0.0) return 59;
+  int e;
+  __builtin_frexp(mx, &e);
   return 59 - e;
 }
 

@@ -795,7 +795,9 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
     }
   }
   __syncthreads();
-  // stage update, elementwise over the block's contiguous state (RK_S5P3 / FiveStageRk)
+  // stage update, elementwise over the block's contiguous state (RK_S5P3 / FiveStageRk):
+  // a streaming loop whose few FP64 operations hide under its memory traffic (the
+  // integer form of fixdot.cuh measured slower here)
   {
     const size_t g0 = (size_t)e0 * NS * 9;
     const int n = cnt * NS * 9;

@@ -112,7 +112,7 @@ def test_error_bound_against_exact_sums(driver, tmp_path, name, C):
     assert worst <= 2.0 ** -52  # one rounding of the result, relative to the terms
 
 
-@pytest.mark.parametrize("name,C", [o for o in OPS if o[0] in ("L5", "M5", "L8", "M8")], ids=lambda o: str(o))
+@pytest.mark.parametrize("name,C", [o for o in OPS if o[0] in ("L5", "M5", "L8", "M8")], ids=["L5", "M5", "L8", "M8"])
 def test_as_accurate_as_an_fp64_chain(driver, tmp_path, name, C):
     """On smooth lines the integer form is at least as close to the exact sums as the FP64
     multiply-add chain it replaces; interpolated values (no cancellation) are mostly
@@ -147,3 +147,4 @@ def test_special_lines(driver, tmp_path):
     assert (Y[3:5] == 0).all() and not np.signbit(Y[3:5]).any()
     # a constant line interpolates to the constant (rows of Lmat sum to 1 within rounding)
     assert np.allclose(Y[5], 1.0, rtol=0, atol=4e-16)
+
