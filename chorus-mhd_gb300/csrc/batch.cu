@@ -100,8 +100,10 @@ __device__ __forceinline__ void for_each_tile(int* counter, int nt, const int4* 
     default: break;                   \
   }
 
-// each cell pass walks its own tile list, cut with that pass's cells per CTA
-__global__ void __launch_bounds__(256) kb_e1(BatchDev b, int slot, int sensor_on) {
+// each cell pass walks its own tile list, cut with that pass's cells per CTA.  The
+// multi-order bodies need more registers than any single order; E1 and E3 are held to
+// 64 (4 and 8 CTAs per SM), which measured faster than fewer CTAs without spills
+__global__ void __launch_bounds__(256, 4) kb_e1(BatchDev b, int slot, int sensor_on) {
   extern __shared__ double sm[];
   pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[0], b.ctiles, b.solves, [&](const int4& T, const SolveDev& s) {
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(256) kb_e2(BatchDev b, int slot) {
                 });
 }
 
-__global__ void __launch_bounds__(128) kb_e3(BatchDev b, int slot, int stage) {
+__global__ void __launch_bounds__(128, 8) kb_e3(BatchDev b, int slot, int stage) {
   extern __shared__ double sm[];
   pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[3], b.ctiles + b.ntiles[0] + b.ntiles[2], b.solves,
@@ -221,6 +223,7 @@ int ctx_device_of(const ChorusCtx* c);
 double ctx_dt(const ChorusCtx* c);
 int ctx_kstage(const ChorusCtx* c);
 int ctx_epb(const ChorusCtx* c, int pass);
+int ctx_threads(const ChorusCtx* c, int pass);
 void ensure_ops_all(int dev, int N, const ChorusCtx* c);
 }  // namespace chorus
 
@@ -426,11 +429,16 @@ int chorus_batch_add(ChorusBatch* b, ChorusCtx* ctx, int32_t* slot) {
   sl.N = sl.sd.N;
   sl.NC = sl.sd.NC;
   sl.nfp_faces = (sl.sd.nface2 + sl.sd.nface1) * sl.N;
-  sl.epb = std::max(1, std::min(ctx_epb(ctx, 2), 64));
-  // the batched E1/E2 run 256 threads per CTA: tiles of at most 8 cells keep their
-  // shared memory (and occupancy) in the range the single-solve shapes were tuned for
-  sl.epb1 = std::max(1, std::min(ctx_epb(ctx, 0), 8));
-  sl.epb2 = std::max(1, std::min(ctx_epb(ctx, 1), 8));
+  // tiles keep the cells-per-thread ratio of the solve's tuned shapes at the batched
+  // kernels' fixed CTA sizes (E1, E2 256 threads, E3 128); E1 and E2 tiles of at most 8
+  // cells keep their shared memory (and occupancy) in the range the shapes were tuned for
+  auto scaled = [&](int pass, int threads, int cap) {
+    const int e = ctx_epb(ctx, pass) * threads / std::max(ctx_threads(ctx, pass), 1);
+    return std::max(1, std::min(e, cap));
+  };
+  sl.epb = scaled(2, 128, 64);
+  sl.epb1 = scaled(0, 256, 8);
+  sl.epb2 = scaled(1, 256, 8);
   sl.epbct = std::max(1, std::min(ctx_epb(ctx, 3), 64));
   sl.dt = ctx_dt(ctx);
   sl.k_stage = ctx_kstage(ctx);

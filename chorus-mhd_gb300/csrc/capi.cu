@@ -187,6 +187,7 @@ int ctx_device_of(const ChorusCtx* c) { return c->device; }
 double ctx_dt(const ChorusCtx* c) { return c->p.dt; }
 int ctx_kstage(const ChorusCtx* c) { return c->p.k_stage; }
 int ctx_epb(const ChorusCtx* c, int pass) { return c->L[pass].epb; }
+int ctx_threads(const ChorusCtx* c, int pass) { return c->L[pass].threads; }
 bool ctx_plot_ready(const ChorusCtx* c) { return c->se6_valid != 0 || !c->sd.artiv; }
 static bool g_ops_all_done[64][kMaxN + 1];
 void ensure_ops_all(int dev, int N, const ChorusCtx* c) {
