@@ -358,23 +358,33 @@ __global__ void __launch_bounds__(512) k_e1(SolveDev s, int epb, int sensor, int
 // cells of this CTA whose gradients (mode 0) or viscous fluxes (mode 1) are needed,
 // compacted into a shared list; returns the count
 __device__ __forceinline__ int active_cells(const SolveDev& s, int e0, int cnt, int mode, int* list) {
+  // the first warp tests 32 cells at a time (their flag loads in flight together) and
+  // compacts them in cell order with a ballot
   __shared__ int n_act;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
     int n = 0;
-    for (int e = 0; e < cnt; e++) {
-      const int c = e0 + e;
-      int need = 1;
-      if (s.skip) {
-        need = s.nv[c];
-        if (mode == 0 && !need) {
-          const int4 b = s.nbr[c];
-          need = (b.x >= 0 && s.nv[b.x]) || (b.y >= 0 && s.nv[b.y]) || (b.z >= 0 && s.nv[b.z]) ||
-                 (b.w >= 0 && s.nv[b.w]);
+    for (int base = 0; base < cnt; base += 32) {
+      const int e = base + lane;
+      int need = 0;
+      if (e < cnt) {
+        const int c = e0 + e;
+        need = 1;
+        if (s.skip) {
+          need = s.nv[c];
+          if (mode == 0) {
+            const int4 b = s.nbr[c];
+            const int nx = b.x >= 0 ? s.nv[b.x] : 0, ny = b.y >= 0 ? s.nv[b.y] : 0;
+            const int nz = b.z >= 0 ? s.nv[b.z] : 0, nw = b.w >= 0 ? s.nv[b.w] : 0;
+            need |= nx | ny | nz | nw;
+          }
         }
       }
-      if (need) list[n++] = e;
+      const unsigned m = __ballot_sync(0xffffffffu, need != 0);
+      if (need) list[n + __popc(m & ((1u << lane) - 1u))] = e;
+      n += __popc(m);
     }
-    n_act = n;
+    if (lane == 0) n_act = n;
   }
   __syncthreads();
   return n_act;
