@@ -20,8 +20,10 @@ import tempfile
 from . import meshgen
 
 PASSES = {"e1": 0, "e2": 2, "e3": 4}  # index into profile_stage's per-kernel times
-EPB_CANDIDATES = [1, 2, 4, 8, 16]
-THREAD_CANDIDATES = [64, 128, 192, 256, 384, 512]
+# every warp multiple: a pass's loops hand out cells x (lines, points) items, and a shape
+# whose item counts fill its warps evenly avoids paying for masked lanes
+EPB_CANDIDATES = [1, 2, 3, 4, 5, 6, 8, 10, 12, 16]
+THREAD_CANDIDATES = list(range(32, 513, 32))
 SMEM_LIMIT = 200 * 1024
 
 
