@@ -224,6 +224,7 @@ double ctx_dt(const ChorusCtx* c);
 int ctx_kstage(const ChorusCtx* c);
 int ctx_epb(const ChorusCtx* c, int pass);
 int ctx_threads(const ChorusCtx* c, int pass);
+void ctx_mark_ct(ChorusCtx* c);
 void ensure_ops_all(int dev, int N, const ChorusCtx* c);
 }  // namespace chorus
 
@@ -491,7 +492,10 @@ int chorus_batch_step(ChorusBatch* b, int32_t nsteps) {
     if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch step: %s", cudaGetErrorString(e));
   }
   for (auto& sl : b->slots)
-    if (sl.ctx && sl.active) sl.steps += nsteps;
+    if (sl.ctx && sl.active) {
+      sl.steps += nsteps;
+      if (nsteps > 0) ctx_mark_ct(sl.ctx);  // each step ends with the CT projection
+    }
   return CHORUS_OK;
 }
 

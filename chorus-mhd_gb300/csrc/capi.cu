@@ -174,6 +174,10 @@ struct ChorusCtx {
   int diagnostics = 1;  // norms every tenth step in iterations_gpu
   int plot_sensor = 0;  // the last stage records the variable-6 sensor (plot etaAV)
   int se6_valid = 0;    // ... and did so in the latest residual evaluation
+  // the CT projection leaves the A_z traces in Azf only: Qvf variable 9 (the reference's
+  // Qvfi(9)/Qvfj(9)) is filled from Azf when it is next read, unless an E1 pass (which
+  // rewrites every Qvf variable) comes first
+  bool qvf9_pending = false;
   std::vector<double> Lmat, Mmat, Xs, Xf;
   // host-state steps: a copy stream and events that chain chunked copies to kernels
   cudaStream_t cp = nullptr;
@@ -189,6 +193,7 @@ int ctx_kstage(const ChorusCtx* c) { return c->p.k_stage; }
 int ctx_epb(const ChorusCtx* c, int pass) { return c->L[pass].epb; }
 int ctx_threads(const ChorusCtx* c, int pass) { return c->L[pass].threads; }
 bool ctx_plot_ready(const ChorusCtx* c) { return c->se6_valid != 0 || !c->sd.artiv; }
+void ctx_mark_ct(ChorusCtx* c) { c->qvf9_pending = true; }
 static bool g_ops_all_done[64][kMaxN + 1];
 void ensure_ops_all(int dev, int N, const ChorusCtx* c) {
   std::lock_guard<std::mutex> lk(g_ops_mu);
@@ -229,6 +234,7 @@ static size_t arena_plan_bytes(int N, int NC, int nface2, int nface1, int k_stag
   P.take<int4>(nface2 + 1); P.take<int2>(nface1 + 1); P.take<FaceNorm>((size_t)nface2 * N + 1);
   P.take<FaceNorm>((size_t)nface1 * N + 1); P.take<unsigned long long>(4); P.take<unsigned int>(4);
   P.take<double>(8); P.take<int>(NC); P.take<int>(NC); P.take<int4>(NC); P.take<int4>(NC);
+  P.take<double>((size_t)NC * NS * 2);
   return P.off;
 }
 
@@ -420,7 +426,8 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
          of2 = P.take<int4>(f2.size() + 1), of1 = P.take<int2>(f1.size() + 1),
          ofn2 = P.take<FaceNorm>(fn2.size() + 1), ofn1 = P.take<FaceNorm>(fn1.size() + 1),
          oeig = P.take<unsigned long long>(4), oerr = P.take<unsigned int>(4), ored = P.take<double>(8),
-         oact = P.take<int>(NC), onv = P.take<int>(NC), onbr = P.take<int4>(NC), onbrlf = P.take<int4>(NC);
+         oact = P.take<int>(NC), onv = P.take<int>(NC), onbr = P.take<int4>(NC), onbrlf = P.take<int4>(NC),
+         onQs9 = P.take<double>((size_t)NC * NS * 2);
   c->arena_bytes = P.off;
   if (P.off != arena_plan_bytes(N, NC, c->nface2, c->nface1, params->k_stage))
     return fail(set_err(CHORUS_EINVAL, "internal: arena plan mismatch"));
@@ -468,6 +475,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   s.nv = (int*)(A + onv);
   s.nbr = (const int4*)(A + onbr);
   s.nbrlf = (const int4*)(A + onbrlf);
+  s.nQs9 = (double*)(A + onQs9);
   c->skip_option = 1;
   s.skip = (params->mu == 0.0 && params->eta0 == 0.0) ? 1 : 0;
   s.eig = (unsigned long long*)(A + oeig);
@@ -623,6 +631,7 @@ namespace {
 void enqueue_stage(ChorusCtx* c, const RKStage& rk, bool last) {
   const SolveDev& s = c->sd;
   c->D->e1(s, c->L[0], c->st, last ? 1 : 0, 0, -1);  // also zeroes the stage's wave speed
+  c->qvf9_pending = false;
   c->D->f1(s, c->st);
   c->D->e2(s, c->L[1], c->st);  // also the face AV viscosities
   c->D->e3(s, rk, c->L[2], c->st);  // averages the grad Q traces where it reads them
@@ -632,6 +641,14 @@ void enqueue_ct(ChorusCtx* c) {
   c->D->ct(c->sd, c->L[3], c->st, 0, 0, -1);
   c->D->ct(c->sd, c->L[3], c->st, 1, 0, -1);
   c->D->ct(c->sd, c->L[3], c->st, 2, 0, -1);
+  c->qvf9_pending = true;
+}
+
+// Qvf variable 9 from Azf, if a CT projection left it pending
+void fill_qvf9(ChorusCtx* c) {
+  if (!c->qvf9_pending) return;
+  launch_qvf9(c->sd, c->st);
+  c->qvf9_pending = false;
 }
 
 RKStage rk_blank() {
@@ -746,6 +763,7 @@ void enqueue_step_host(ChorusCtx* c, bool diag, const double* Qin, double* Qout)
   } else {
     c->D->ct(s, c->L[3], c->st, 2, 0, -1);
   }
+  c->qvf9_pending = true;
   if (diag) enqueue_diag(c);  // reads Q only: it may overlap the download
 }
 
@@ -803,6 +821,7 @@ int comp_inviscid_flux_gpu(ChorusCtx* c) {
   if (!c) return set_err(CHORUS_EINVAL, "null context");
   if (ctx_device(c)) return CHORUS_ECUDA;
   c->D->e1ns(c->sd, c->L[0], c->st);
+  c->qvf9_pending = false;
   c->D->f1(c->sd, c->st);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
@@ -813,6 +832,7 @@ int nablaqsp_gpu(ChorusCtx* c, const int32_t* v_sta, const int32_t* v_end) {
   if (!c || !v_sta || !v_end) return set_err(CHORUS_EINVAL, "null argument");
   if (*v_sta < 1 || *v_end > 9 || *v_sta > *v_end) return set_err(CHORUS_EINVAL, "variable range %d..%d", *v_sta, *v_end);
   if (ctx_device(c)) return CHORUS_ECUDA;
+  if (*v_end == 9) fill_qvf9(c);  // nablaQsp(9,9) reads the A_z traces
   c->D->nqsp(c->sd, *v_sta - 1, *v_end - 1, c->st);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
@@ -924,7 +944,10 @@ static int run_steps(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime,
   int rc = flush();
   if (rc) return rc;
   if (n_diag) *n_diag = nd;
-  if (nsteps > 0) c->se6_valid = c->plot_sensor;
+  if (nsteps > 0) {
+    c->se6_valid = c->plot_sensor;
+    c->qvf9_pending = true;  // every step ends with the CT projection
+  }
   if (Qout) CK(cudaStreamSynchronize(c->cp));
   return check_err_flag(c);
 }
@@ -957,6 +980,7 @@ int chorus_gpu_profile_stage(ChorusCtx* c, int32_t reps, double* ms) {
     CK(cudaMemsetAsync(s.eig, 0, sizeof(unsigned long long), c->st));
     CK(cudaEventRecord(ev[0], c->st));
     c->D->e1(s, c->L[0], c->st, 0, 0, -1);
+    c->qvf9_pending = false;
     CK(cudaEventRecord(ev[1], c->st));
     c->D->f1(s, c->st);
     CK(cudaEventRecord(ev[2], c->st));
@@ -1014,6 +1038,14 @@ int chorus_gpu_download_array(ChorusCtx* c, const char* name, double* out, int64
       if ((size_t)count != x.cnt) return set_err(CHORUS_EINVAL, "%s has %zu elements, not %lld", name, x.cnt, (long long)count);
       CK(cudaMemcpyAsync(out, x.p, x.cnt * sizeof(double), cudaMemcpyDeviceToHost, c->st));
       CK(cudaStreamSynchronize(c->st));
+      if (x.p == s.nQs) {  // variable 9 lives in its own array
+        int rc = pull(s.nQs9, (size_t)NC * NS * 2, h);
+        if (rc) return rc;
+        for (size_t pt = 0; pt < (size_t)NC * NS; pt++) {
+          out[pt * 18 + 8] = h[2 * pt];
+          out[pt * 18 + 17] = h[2 * pt + 1];
+        }
+      }
       if (n == "SM_IND1")  // the device keeps the sensor sum; Se = log10(sum) (AV.f90:79)
         for (size_t i = 0; i < x.cnt; i++) out[i] = std::log10(out[i]);
       return CHORUS_OK;
@@ -1027,6 +1059,7 @@ int chorus_gpu_download_array(ChorusCtx* c, const char* name, double* out, int64
       // the stage averages the grad Q traces where it reads them: store the averages
       // (idempotent) so that the arrays equal the reference's nablaQvfi / nablaQvfj
       if (x.p == s.nQvf) c->D->f2(s, c->st);
+      if (x.p == s.Qvf) fill_qvf9(c);
       const size_t per = (size_t)NF1 * x.w;
       if ((size_t)count != per * NC) return set_err(CHORUS_EINVAL, "%s has %zu elements", name, per * NC);
       int rc = pull(x.p, (size_t)NC * NFP * x.w, h);

@@ -95,7 +95,7 @@ struct SolveDev {
   unsigned int* err;            // error flags (bit 0: non-finite wave speed)
   double* diag;                 // per-cell diagnostic partial sums [e][2]
   const int* plot_flag;         // nonzero: the last stage records Se6 (read by E1 at run time)
-  void* pad3;                   // keeps the size a multiple of 16 bytes
+  double* nQs9;                 // [e][sp][2] grad A_z of variable 9 (nablaQs(9,:,...)), kept apart from nQs
 };
 
 // One RK stage update: Qnew = sum_j c[j]*src[j] + cQ*Q + cR*R (+ cR0*R0), with
@@ -151,5 +151,6 @@ void launch_point_vflux_av(int n, double gam, const PointAxes& ax, const double*
                            const int* jfp, const int* ic, const double* Qv, const double* nQ, double* Fv, double* Gv,
                            cudaStream_t st);
 void launch_reduce_diag(const double* diag, int NC, double* out2, cudaStream_t st);
+void launch_qvf9(const SolveDev& s, cudaStream_t st);  // Qvf variable 9 from Azf (point.cu)
 
 }  // namespace chorus

@@ -856,8 +856,9 @@ __global__ void __launch_bounds__(512) k_e3(SolveDev s, RKStage rk, int epb, int
 template <int N, class O>
 __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt, int epb, int mode, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
-  // A_z traces live twice: in Qvf variable 9 (the reference's Qvfi(9)/Qvfj(9), which
-  // nablaQsp(9,9) reads) and compactly in Azf, which the gradient below reads coalesced
+  // the A_z traces go to Azf only, which the gradient below reads coalesced; the
+  // reference's Qvfi(9)/Qvfj(9) are filled from Azf where they are read (downloads,
+  // nablaQsp(9,9)), so the pass makes no strided writes into Qvf
   if (mode == 0) {
     double* sA = sm;  // [epb][NS] A_z at the solution points
     for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sA[i] = s.Q[((size_t)e0 * NS + i) * 9 + 8];
@@ -890,12 +891,8 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
           Od += O::ops().CO[f * kHalfS + j] * od[j];
         }
         const size_t ga = g0 + f0 + f * fs, gb = g0 + f0 + (N - f) * fs;
-        s.Qvf[ga * 9 + 8] = E + Od;
         s.Azf[ga] = E + Od;
-        if (f != N - f) {
-          s.Qvf[gb * 9 + 8] = E - Od;
-          s.Azf[gb] = E - Od;
-        }
+        if (f != N - f) s.Azf[gb] = E - Od;
       }
     }
   } else {
@@ -921,7 +918,7 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
       }
       const size_t gs = (size_t)e0 * NS + ep;
       a *= s.invJ[gs];
-      s.nQs[gs * 18 + 9 * c + 8] = a;
+      s.nQs9[gs * 2 + c] = a;
       if (c) s.Q[gs * 9 + 5] = a + s.B0x;    // Bx = dA/dy
       else s.Q[gs * 9 + 6] = -a + s.B0y;     // By = -dA/dx
     }
@@ -947,8 +944,6 @@ __device__ __forceinline__ void ctface_point(const SolveDev& s, int t) {
   const size_t gl = (size_t)fc.x * NFP + face_fp<N>(fc.y, nfp);
   const size_t gr = (size_t)fc.z * NFP + face_fp<N>(fc.w, N - 1 - nfp);
   const double v = half(s.Azf[gl] + s.Azf[gr]);
-  s.Qvf[gl * 9 + 8] = v;
-  s.Qvf[gr * 9 + 8] = v;
   s.Azf[gl] = v;
   s.Azf[gr] = v;
 }
@@ -1049,8 +1044,13 @@ __global__ void __launch_bounds__(256) k_nqsp(SolveDev s, int v0, int v1) {
       gy += w[(2 * (N + 1) + r) * NS] * fa;
       gy += w[(3 * (N + 1) + r) * NS] * fb;
     }
-    s.nQs[(size_t)t * 18 + k] = gx;
-    s.nQs[(size_t)t * 18 + 9 + k] = gy;
+    if (k < 8) {
+      s.nQs[(size_t)t * 18 + k] = gx;
+      s.nQs[(size_t)t * 18 + 9 + k] = gy;
+    } else {  // variable 9 is kept in its own array (SolveDev::nQs9)
+      s.nQs9[(size_t)t * 2] = gx;
+      s.nQs9[(size_t)t * 2 + 1] = gy;
+    }
   }
 }
 

@@ -125,6 +125,17 @@ void launch_point_vflux_av(int n, double gam, const PointAxes& ax, const double*
   if (n > 0)
     k_point_vflux_av<<<(n + 127) / 128, 128, 0, st>>>(n, gam, ax, muf, fam, ifp, jfp, ic, Qv, nQ, Fv, Gv);
 }
+// Qvf variable 9 (the reference's Qvfi(9)/Qvfj(9)) from the compact A_z traces
+__global__ void k_qvf9(const double* Azf, double* Qvf, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) Qvf[i * 9 + 8] = Azf[i];
+}
+
+void launch_qvf9(const SolveDev& s, cudaStream_t st) {
+  const size_t n = (size_t)s.NC * 2 * (s.N + 1) * s.N;
+  if (n > 0) k_qvf9<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s.Azf, s.Qvf, n);
+}
+
 void launch_reduce_diag(const double* diag, int NC, double* out2, cudaStream_t st) {
   k_reduce_diag<<<1, 1024, 0, st>>>(diag, NC, out2);
 }

@@ -122,7 +122,11 @@ int comp_inviscid_flux_gpu(ChorusCtx* ctx);
 /* compflux.f90:107-157 nablaQsp(v_sta,v_end) on the current Qvfi/Qvfj (1-based
  * variable range, by reference like the Fortran call). */
 int nablaqsp_gpu(ChorusCtx* ctx, const int32_t* v_sta, const int32_t* v_end);
-/* setinitialcond.f90:82-91 correct_B_via_curl_Az (CT projection B <- curl A_z). */
+/* setinitialcond.f90:82-91 correct_B_via_curl_Az (CT projection B <- curl A_z).  Afterwards
+ * Q's B_x, B_y, the face-averaged A_z traces Qvfi(9)/Qvfj(9) (also in "Azfi"/"Azfj") and
+ * nablaQs(9,:) hold the projection's values; the other work arrays keep their contents
+ * (the reference's inner comp_inviscid_flux also refreshes F1/G2, Qvfi(1:8) and the upwinded
+ * Azfi/Azfj: call comp_inviscid_flux_gpu for those). */
 int correct_b_via_curl_az_gpu(ChorusCtx* ctx);
 /* iterations.f90:162-217 RK_S5P3 and :92-160 FiveStageRk: one 5-stage step with the
  * bound dt; *ctime is advanced exactly as the reference does. */

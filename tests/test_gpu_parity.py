@@ -126,6 +126,60 @@ def test_drop_in_sequence_matches_oracle(case_root):
     assert s.ctime == pytest.approx(o.getd("ctime"), rel=1e-15)
 
 
+@pytest.mark.parametrize("spec", [dict(problem="orszag_tang", nx=6, ny=5, N=4, jitter=0.1, seed=17),
+                                  dict(problem="rotor", nx=64, ny=64, N=3, jitter=0.1, seed=6)],
+                         ids=["orszag_tang", "rotor_free"])
+def test_ct_projection_arrays_match_oracle(case_root, spec):
+    """After correct_B_via_curl_Az, alone and at the end of graph-replayed steps, the
+    arrays the projection defines match the oracle: the state (B), the face-averaged A_z
+    traces of Qvfi(9)/Qvfj(9) and nablaQs(9,:) (kept apart on the device and merged where
+    they are read), also through nablaQsp(9,9) and after further drop-in calls."""
+    d = make_case(case_root, **spec)
+    o = oracle.Oracle(d)
+    o.run(2)
+    Q = o.array("Q").copy()
+    s = Solver(Mesh(d), initial_state=False)
+    s.upload(Q)
+    o.correct_B_via_curl_Az()
+    s.correct_B_via_curl_Az()
+    sz = reference_layout_sizes(s.N, s.ncell)
+
+    def var9(name):
+        a = s.array(name, sz[name]).reshape(-1, 9)[:, 8]
+        b = o.array(name).reshape(-1, 9)[:, 8]
+        return a, b
+
+    assert_close(s.state(), o.array("Q"), STAGE_TOL, "Q after the projection")
+    for name in ("Qvfi", "Qvfj", "nablaQs"):
+        a, b = var9(name)
+        assert_close(a, b, STAGE_TOL, name + "(9)")
+    # nablaQsp(9,9) recomputes variable 9 from the (pending) traces
+    s.nablaQsp(9, 9)
+    o.nablaQsp(9, 9)
+    a, b = var9("nablaQs")
+    assert_close(a, b, STAGE_TOL, "nablaQs(9) after nablaQsp(9,9)")
+    # a residual evaluation rewrites every Qvf variable; nablaQs(9) keeps the projection's
+    s.compresid()
+    o.compresid()
+    for name in ("Qvfi", "Qvfj", "nablaQs"):
+        a, b = var9(name)
+        assert_close(a, b, STAGE_TOL, name + "(9) after compresid")
+    # graph-replayed steps end with the projection
+    s2 = Solver(Mesh(d), initial_state=False)
+    s2.upload(Q)
+    o2 = oracle.Oracle(d)
+    o2.array("Q")[:] = Q
+    for _ in range(3):
+        o2.step()
+    s2.iterations(3)
+    for name in ("Qvfi", "Qvfj", "nablaQs"):
+        a = s2.array(name, sz[name]).reshape(-1, 9)[:, 8]
+        b = o2.array(name).reshape(-1, 9)[:, 8]
+        assert_close(a, b, RUN_TOL, name + "(9) after steps")
+    for x in (s, s2):
+        x.close()
+
+
 @pytest.mark.parametrize("case", [c for c in CASES if c.get("artiv", 1) and not c.get("mu")], ids=ids)
 def test_skipping_inactive_viscous_work_changes_nothing(case_root, case):
     """With mu = eta0 = 0 the skipped work is an exact zero: the residual with skipping
