@@ -677,7 +677,7 @@ template <int N, class O>
 __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int epb, const RKStage& rk, int update, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
 
-  double* sF = sm;                  // [epb][NFP][8] total flux Fv - F
+  double* sF = sm;                  // [epb][NFP][8] F - Fv, the negated total flux
   double* sD = sF + epb * NFP * 8;  // [epb][NS] diagnostic partial sums
   double* sR = sD + epb * NS;       // [epb][NS][9] residual
   double* sJ = sR + epb * NS * 9;   // [epb][NS] 1/J
@@ -691,7 +691,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
     // block's contiguous state)
     const double* fi = s.Fc + (size_t)e0 * NFP * 8;
 #pragma unroll 4
-    for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) sF[i] = -fi[i];
+    for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) sF[i] = fi[i];
     for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sJ[i] = s.invJ[(size_t)e0 * NS + i];
     for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
       const size_t g = (size_t)e0 * NFP + i;
@@ -748,7 +748,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
       vflux_contra(q, gq, mut, s.eta0, s.gam, s.met[2 * g], s.met[2 * g + 1], Fv);
       double* d = sF + (e * NFP + fp) * 8;
 #pragma unroll
-      for (int k = 1; k < 8; k++) d[k] += Fv[k];
+      for (int k = 1; k < 8; k++) d[k] -= Fv[k];
     }
   }
   __syncthreads();
@@ -775,11 +775,11 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
       const int os = fl ? ps * 9 : ps * 2;
       if (!fam) {
 #pragma unroll
-        for (int i = 0; i < N; i++) out[i * os] = y[i];
+        for (int i = 0; i < N; i++) out[i * os] = fl ? negate(y[i]) : y[i];  // the flux enters negated
       } else {
 #pragma unroll
         for (int i = 0; i < N; i++) {
-          const double a = (out[i * os] + y[i]) * sJ[p0 + i * ps];
+          const double a = (fl ? out[i * os] - y[i] : out[i * os] + y[i]) * sJ[p0 + i * ps];
           out[i * os] = a;
           if (!fl) s.nAs[((size_t)e0 * NS + p0 + i * ps) * 2 + (k - 8)] = a;
         }
@@ -792,7 +792,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
     const double* q = s.Q + ((size_t)e0 * NS + t) * 9;
     const double ri = rcp_pos(q[0]);
     const double ax = sN[2 * t] - s.B0y, ay = sN[2 * t + 1] + s.B0x;
-    sR[t * 9 + 8] = -(q[1] * ri * ax + q[2] * ri * ay);
+    sR[t * 9 + 8] = negate(q[1] * ri * ax + q[2] * ri * ay);
   }
   if (rk.diag) {
     __syncthreads();

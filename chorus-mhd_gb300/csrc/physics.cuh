@@ -42,6 +42,16 @@ __host__ __device__ __forceinline__ double half(double x) {
 #endif
 }
 
+// -x as a sign-bit flip: a negation that no add or multiply absorbs would otherwise
+// take an FP64 instruction
+__host__ __device__ __forceinline__ double negate(double x) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+#else
+  return -x;
+#endif
+}
+
 // x * s for s = +-1 as a sign-bit flip (integer pipe, exact)
 __host__ __device__ __forceinline__ double times_sign(double x, double s) {
 #ifdef __CUDA_ARCH__
