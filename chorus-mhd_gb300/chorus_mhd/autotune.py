@@ -37,7 +37,7 @@ def cache_path(gpu_name: str) -> str:
 
 def _smem_bytes(N: int, pass_: str, epb: int) -> int:
     NS, NFP = N * N, 2 * (N + 1) * N
-    per = {"e1": NS * 9 + 2 * NS + NFP * 9, "e2": NFP * 9 + 4 * (N + 1) * NS + NS * 16,
+    per = {"e1": NS * 9 + 2 * NS + NFP * 9, "e2": NFP * 16 + NS * 17,
            "e3": NFP * 10 + NS * 13}[pass_]
     return 8 * (epb * per + (NS if pass_ == "e1" else 0))
 

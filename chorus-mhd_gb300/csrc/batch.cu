@@ -187,7 +187,7 @@ size_t cell_smem_bytes(int N, int epb, int pass) {
   size_t d = 0;
   switch (pass) {
     case 0: d = (size_t)epb * (NS * 9 + 2 * NS + NFP * 9) + N * N; break;
-    case 1: d = (size_t)epb * (NFP * 9 + 4 * (N + 1) * NS + NS * 16); break;
+    case 1: d = (size_t)epb * (NFP * 16 + NS * 17); break;
     case 2: d = (size_t)epb * (NFP * 8 + NS * (1 + 9 + 1 + 2) + NFP * 2); break;
     default: d = (size_t)epb * NFP * 2; break;
   }

@@ -182,6 +182,70 @@ __device__ __forceinline__ int interior_fp(int i) {
   return D<N>::NF1 + jfp * N + ifp;
 }
 
+// interpolation along one line from the N solution values to the N+1 flux points,
+// y_f = sum_j L(f,j) v_j: the integer form (fixdot.cuh), or FP64 for a line with
+// non-finite or huge values, where the mirror symmetry of the points halves the
+// multiplications (see OpsN::CE)
+template <int N, class O>
+__device__ __forceinline__ void interp_line(const double (&v)[N], double (&y)[N + 1]) {
+  const int emax = fix_emax(v);
+  if (emax <= kFixEmaxFast) {
+    int h[N], l[N];
+    fix_align(v, emax, h, l);
+    const int sc = emax - 1017 - kFixG - O::ops().LS;
+#pragma unroll
+    for (int f = 0; f <= N; f++) y[f] = fix_dot(h, l, O::ops().LH + f * N, O::ops().LL + f * N, sc);
+    return;
+  }
+  double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
+#pragma unroll
+  for (int j = 0; j < N / 2; j++) {
+    ev[j] = v[j] + v[N - 1 - j];
+    od[j] = v[j] - v[N - 1 - j];
+  }
+#pragma unroll
+  for (int f = 0; f <= N / 2; f++) {
+    double E = (N & 1) ? O::ops().LMID[f] * v[(N - 1) / 2] : 0.0;
+    double Od = 0.0;
+#pragma unroll
+    for (int j = 0; j < N / 2; j++) {
+      E += O::ops().CE[f * kHalfS + j] * ev[j];
+      Od += O::ops().CO[f * kHalfS + j] * od[j];
+    }
+    y[f] = E + Od;
+    if (f != N - f) y[N - f] = E - Od;
+  }
+}
+
+// the derivative along one line, y_i = sum_r M(r,i) x_r (i < N) from the N+1 flux values
+// x_r = x[r*xs]: the integer form (fixdot.cuh), or FP64 for a line with non-finite or
+// huge values
+template <int N, class O>
+__device__ __forceinline__ void deriv_line(const double* x, int xs, double (&y)[N]) {
+  double v[N + 1];
+#pragma unroll
+  for (int r = 0; r <= N; r++) v[r] = x[r * xs];
+  const int emax = fix_emax(v);
+  if (emax <= kFixEmaxFast) {
+    int h[N + 1], l[N + 1];
+    fix_align(v, emax, h, l);
+    const int sc = emax - 1017 - kFixG - O::ops().MS;
+#pragma unroll
+    for (int i = 0; i < N; i++) y[i] = fix_dot(h, l, O::ops().MH + i * (N + 1), O::ops().ML + i * (N + 1), sc);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      double a = 0.0;
+#pragma unroll
+      for (int r = 0; r <= N; r++) a += O::ops().M[r + (N + 1) * i] * v[r];
+      y[i] = a;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// E3: viscous + AV flux, divergence, A_z advection, RK update
+// ---------------------------------------------------------------------------
 template <int N, class O>
 __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int epb, int sensor, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NINT = 2 * N * (N - 1);
@@ -198,10 +262,8 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
   }
   __syncthreads();
   // interpolation to every flux point, one (cell, line, variable) per thread so that
-  // every lane of every warp does work.  The line operator runs on the integer pipes
-  // (fixdot.cuh), which the FP64 work of the pass leaves idle; lines with non-finite or
-  // huge values keep the FP64 form, where the mirror symmetry of the points halves the
-  // multiplications (see OpsN::CE)
+  // every lane of every warp does work; the line operator runs on the integer pipes,
+  // which the FP64 work of the pass leaves idle
   for (int t = threadIdx.x; t < cnt * 2 * N * 9; t += blockDim.x) {
     const int k = t % 9, el = t / 9, e = el / (2 * N), line = el - e * 2 * N;
     const double* q = sQ + e * NS * 9 + k;
@@ -212,36 +274,12 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
     const int qs = fam1 ? 9 : N * 9;
     double* ob = sV + (e * NFP + (fam1 ? ln * (N + 1) : NF1 + ln)) * 9 + k;
     const int os = fam1 ? 9 : N * 9;
-    double v[N];
+    double v[N], y[N + 1];
 #pragma unroll
     for (int sp = 0; sp < N; sp++) v[sp] = qb[sp * qs];
-    const int emax = fix_emax(v);
-    if (emax <= kFixEmaxFast) {
-      int h[N], l[N];
-      fix_align(v, emax, h, l);
-      const int sc = emax - 1017 - kFixG - O::ops().LS;
+    interp_line<N, O>(v, y);
 #pragma unroll
-      for (int f = 0; f <= N; f++) ob[f * os] = fix_dot(h, l, O::ops().LH + f * N, O::ops().LL + f * N, sc);
-      continue;
-    }
-    double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
-#pragma unroll
-    for (int j = 0; j < N / 2; j++) {
-      ev[j] = v[j] + v[N - 1 - j];
-      od[j] = v[j] - v[N - 1 - j];
-    }
-#pragma unroll
-    for (int f = 0; f <= N / 2; f++) {
-      double E = (N & 1) ? O::ops().LMID[f] * v[(N - 1) / 2] : 0.0;
-      double Od = 0.0;
-#pragma unroll
-      for (int j = 0; j < N / 2; j++) {
-        E += O::ops().CE[f * kHalfS + j] * ev[j];
-        Od += O::ops().CO[f * kHalfS + j] * od[j];
-      }
-      ob[f * os] = E + Od;
-      if (f != N - f) ob[(N - f) * os] = E - Od;
-    }
+    for (int f = 0; f <= N; f++) ob[f * os] = y[f];
   }
   __syncthreads();
   // contravariant inviscid flux at the interior flux points only (face points of Fc and
@@ -493,46 +531,55 @@ __device__ __forceinline__ void cell_face_mu(const SolveDev& s, int c) {
 template <int N, class O>
 __device__ __forceinline__ void e2_cells(const SolveDev& s, const int* cells, int n, double* sm) {
   // gradients of the n (<= epb) listed cells; grad A_z (nablaAsp) is computed with the
-  // divergence in the last pass.  Every loop hands one (cell, point, variable) or (cell,
-  // line, component) item to each thread, so that all lanes issue FP64 work.
-  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
-  double* sQ = sm;                // [n][NFP][9] face-corrected flux-point states
-  double* sW = sQ + n * NFP * 9;  // [n][NG][NS] gradient weights (gco)
-  double* sG = sW + n * NG * NS;  // [n][NS][16] grad Q (d*8 + k)
-  for (int i = threadIdx.x; i < n * NFP * 9; i += blockDim.x) {
-    const int le = i / (NFP * 9), r = i - le * (NFP * 9);
-    sQ[i] = s.Qvf[(size_t)cells[le] * NFP * 9 + r];
+  // divergence in the last pass.  nablaQsp (compflux.f90:107-157) in its conservative
+  // form: grad_x Q = (1/J) [d/dxi (S1(1,1) Q) + d/deta (S2(2,1) Q)], grad_y the same with
+  // the second metric entries, i.e. the divergence of the products of the face-corrected
+  // flux-point states with the metric terms, differentiated along the lines on the
+  // integer pipes as in E3.
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
+  double* sP = sm;                // [n][NFP][16] Q_k * (S_x, S_y): k + 8 d
+  double* sG = sP + n * NFP * 16;  // [n][NS][16] grad Q (d*8 + k)
+  double* sJ = sG + n * NS * 16;   // [n][NS] 1/J
+  for (int i = threadIdx.x; i < n * NFP * 8; i += blockDim.x) {
+    const int le = i / (NFP * 8), r = i - le * (NFP * 8), fp = r >> 3, k = r & 7;
+    const size_t g = (size_t)cells[le] * NFP + fp;
+    const double q = s.Qvf[g * 9 + k];
+    sP[(le * NFP + fp) * 16 + k] = q * s.met[2 * g];
+    sP[(le * NFP + fp) * 16 + 8 + k] = q * s.met[2 * g + 1];
   }
-  for (int i = threadIdx.x; i < n * NG * NS; i += blockDim.x) {
-    const int le = i / (NG * NS), r = i - le * (NG * NS);
-    sW[i] = s.gco[(size_t)cells[le] * NG * NS + r];
+  for (int i = threadIdx.x; i < n * NS; i += blockDim.x) {
+    const int le = i / NS, p = i - le * NS;
+    sJ[i] = s.invJ[(size_t)cells[le] * NS + p];
   }
   __syncthreads();
-  // grad Q (variables 1-8) at the solution points (nablaQsp): one (cell, point,
-  // variable) per thread, both components
-  for (int t = threadIdx.x; t < n * NS * 8; t += blockDim.x) {
-    const int k = t & 7, lp = t >> 3, le = lp / NS, p = lp - le * NS, is = p % N, js = p / N;
-    const double* w = sW + le * NG * NS + p;
-    const double* q = sQ + le * NFP * 9 + k;
-    double gx = 0.0, gy = 0.0;
+  // grad Q (variables 1-8) at the solution points: one (cell, line, quantity) per thread,
+  // the xi lines first, then the eta lines adding to them and scaling by 1/J
+#pragma unroll 1
+  for (int fam = 0; fam < 2; fam++) {
+    for (int t = threadIdx.x; t < n * N * 16; t += blockDim.x) {
+      const int c = t & 15, el = t >> 4, le = el / N, ln = el - le * N;
+      const int fp0 = fam ? NF1 + ln : ln * (N + 1), fps = fam ? N : 1;
+      double y[N];
+      deriv_line<N, O>(sP + (le * NFP + fp0) * 16 + c, fps * 16, y);
+      const int p0 = fam ? ln : ln * N, ps = fam ? N : 1;
+      double* g = sG + (le * NS + p0) * 16 + c;
+      if (!fam) {
 #pragma unroll
-    for (int r = 0; r <= N; r++) {
-      const double a = q[(js * (N + 1) + r) * 9];
-      const double b = q[(NF1 + r * N + is) * 9];
-      gx += w[r * NS] * a;
-      gx += w[((N + 1) + r) * NS] * b;
-      gy += w[(2 * (N + 1) + r) * NS] * a;
-      gy += w[(3 * (N + 1) + r) * NS] * b;
+        for (int i = 0; i < N; i++) g[i * ps * 16] = y[i];
+      } else {
+        double* out = s.nQs + ((size_t)cells[le] * NS + p0) * 18 + (c < 8 ? c : c + 1);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+          const double a = (g[i * ps * 16] + y[i]) * sJ[le * NS + p0 + i * ps];
+          g[i * ps * 16] = a;
+          out[(size_t)i * ps * 18] = a;
+        }
+      }
     }
-    double* out = s.nQs + ((size_t)cells[le] * NS + p) * 18;
-    out[k] = gx;
-    out[9 + k] = gy;
-    sG[lp * 16 + k] = gx;
-    sG[lp * 16 + 8 + k] = gy;
+    __syncthreads();
   }
-  __syncthreads();
   // grad Q at every flux point (nablaQ_interior_FP + face traces): one (cell, line,
-  // component) per thread, the mirror symmetry of the points as in E1
+  // component) per thread, the line operator on the integer pipes as in E1
   for (int t = threadIdx.x; t < n * 2 * N * 16; t += blockDim.x) {
     const int c = t & 15, el = t >> 4, le = el / (2 * N), line = el - le * 2 * N;
     const bool fam1 = line < N;
@@ -541,27 +588,12 @@ __device__ __forceinline__ void e2_cells(const SolveDev& s, const int* cells, in
     const int gs = fam1 ? 16 : N * 16;
     const int f0 = fam1 ? ln * (N + 1) : NF1 + ln, fs = fam1 ? 1 : N;
     double* ob = s.nQvf + ((size_t)cells[le] * NFP + f0) * 18 + (c < 8 ? c : c + 1);
-    double v[N];
+    double v[N], y[N + 1];
 #pragma unroll
     for (int sp = 0; sp < N; sp++) v[sp] = gb[sp * gs];
-    double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
+    interp_line<N, O>(v, y);
 #pragma unroll
-    for (int j = 0; j < N / 2; j++) {
-      ev[j] = v[j] + v[N - 1 - j];
-      od[j] = v[j] - v[N - 1 - j];
-    }
-#pragma unroll
-    for (int f = 0; f <= N / 2; f++) {
-      double E = (N & 1) ? O::ops().LMID[f] * v[(N - 1) / 2] : 0.0;
-      double Od = 0.0;
-#pragma unroll
-      for (int j = 0; j < N / 2; j++) {
-        E += O::ops().CE[f * kHalfS + j] * ev[j];
-        Od += O::ops().CO[f * kHalfS + j] * od[j];
-      }
-      ob[(size_t)f * fs * 18] = E + Od;
-      if (f != N - f) ob[(size_t)(N - f) * fs * 18] = E - Od;
-    }
+    for (int f = 0; f <= N; f++) ob[(size_t)f * fs * 18] = y[f];
   }
 }
 
@@ -644,35 +676,6 @@ __global__ void __launch_bounds__(256) k_f2(SolveDev s) {
   f2_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// the derivative along one line, y_i = sum_r M(r,i) x_r (i < N) from the N+1 flux values
-// x_r = x[r*xs]: the integer form (fixdot.cuh), or FP64 for a line with non-finite or
-// huge values
-template <int N, class O>
-__device__ __forceinline__ void deriv_line(const double* x, int xs, double (&y)[N]) {
-  double v[N + 1];
-#pragma unroll
-  for (int r = 0; r <= N; r++) v[r] = x[r * xs];
-  const int emax = fix_emax(v);
-  if (emax <= kFixEmaxFast) {
-    int h[N + 1], l[N + 1];
-    fix_align(v, emax, h, l);
-    const int sc = emax - 1017 - kFixG - O::ops().MS;
-#pragma unroll
-    for (int i = 0; i < N; i++) y[i] = fix_dot(h, l, O::ops().MH + i * (N + 1), O::ops().ML + i * (N + 1), sc);
-  } else {
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-      double a = 0.0;
-#pragma unroll
-      for (int r = 0; r <= N; r++) a += O::ops().M[r + (N + 1) * i] * v[r];
-      y[i] = a;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// E3: viscous + AV flux, divergence, A_z advection, RK update
-// ---------------------------------------------------------------------------
 template <int N, class O>
 __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int epb, const RKStage& rk, int update, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;

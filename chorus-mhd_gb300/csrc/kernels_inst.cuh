@@ -16,7 +16,7 @@ inline size_t smem_e1(int epb) {
   return sizeof(double) * ((size_t)epb * (D<kN>::NS * 9 + 2 * D<kN>::NS + D<kN>::NFP * 9) + kN * kN);
 }
 inline size_t smem_e2(int epb) {
-  return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 9 + D<kN>::NG * D<kN>::NS + D<kN>::NS * 16));
+  return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 16 + D<kN>::NS * 17));
 }
 inline size_t smem_e3(int epb) {
   return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 8 + D<kN>::NS * (1 + 9 + 1 + 2) + D<kN>::NFP * 2));
