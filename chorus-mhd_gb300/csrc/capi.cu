@@ -222,14 +222,14 @@ struct ArenaPlan {
 
 // bytes of one solve's device arena (the same allocation sequence as chorus_gpu_bind)
 static size_t arena_plan_bytes(int N, int NC, int nface2, int nface1, int k_stage) {
-  const int NS = N * N, NFP = 2 * (N + 1) * N, NG = 4 * (N + 1);
+  const int NS = N * N, NFP = 2 * (N + 1) * N;
   const size_t nq = (size_t)NC * NS * 9, nfp = (size_t)NC * NFP;
   ArenaPlan P;
   P.take<double>(nq); P.take<double>(nq); P.take<double>(nq);
   if (k_stage == 5) { P.take<double>(nq); P.take<double>(nq); P.take<double>(nq); }
   P.take<double>(nq); P.take<double>(nfp * 9); P.take<double>(nfp * 8); P.take<double>(nfp);
   P.take<double>((size_t)NC * NS * 18); P.take<double>(nfp * 18); P.take<double>((size_t)NC * NS * 2);
-  P.take<double>(nfp * 2); P.take<double>((size_t)NC * NS * NG); P.take<double>((size_t)NC * NS);
+  P.take<double>(nfp * 2); P.take<double>((size_t)NC * NS);
   P.take<double>((size_t)NC * 2); P.take<double>((size_t)NC * 4); P.take<double>((size_t)NC * 2);
   P.take<int4>(nface2 + 1); P.take<int2>(nface1 + 1); P.take<FaceNorm>((size_t)nface2 * N + 1);
   P.take<FaceNorm>((size_t)nface1 * N + 1); P.take<unsigned long long>(4); P.take<unsigned int>(4);
@@ -345,7 +345,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   }
 
   // ---- derived geometry
-  const int NS = N * N, NF1 = (N + 1) * N, NFP = 2 * NF1, NG = 4 * (N + 1);
+  const int NS = N * N, NF1 = (N + 1) * N, NFP = 2 * NF1;
   auto S1at = [&](int a, int b, int ifp, int jfp, int ic) {
     return S1[a + 2 * (b + 2 * (ifp + (N + 1) * (jfp + (size_t)N * ic)))];
   };
@@ -353,7 +353,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
     return S2[a + 2 * (b + 2 * (ifp + N * (jfp + (size_t)(N + 1) * ic)))];
   };
   auto Jat = [&](int is, int js, int ic) { return Jac[is + N * (js + (size_t)N * ic)]; };
-  std::vector<double> met((size_t)NC * NFP * 2), gco((size_t)NC * NS * NG), invJ((size_t)NC * NS);
+  std::vector<double> met((size_t)NC * NFP * 2), invJ((size_t)NC * NS);
   for (int ic = 0; ic < NC; ic++) {
     for (int jfp = 0; jfp < N; jfp++)
       for (int ifp = 0; ifp <= N; ifp++) {
@@ -375,14 +375,6 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
           return fail(code);
         }
         invJ[(size_t)ic * NS + js * N + is] = 1.0 / J;
-        // [cell][weight][point]: a warp reading one weight of consecutive points is coalesced
-        double* w = &gco[(size_t)ic * NG * NS + js * N + is];
-        for (int r = 0; r <= N; r++) {
-          w[(size_t)r * NS] = Mmat[r + (N + 1) * is] * S1at(0, 0, r, js, ic) / J;
-          w[(size_t)((N + 1) + r) * NS] = Mmat[r + (N + 1) * js] * S2at(1, 0, is, r, ic) / J;
-          w[(size_t)(2 * (N + 1) + r) * NS] = Mmat[r + (N + 1) * is] * S1at(0, 1, r, js, ic) / J;
-          w[(size_t)(3 * (N + 1) + r) * NS] = Mmat[r + (N + 1) * js] * S2at(1, 1, is, r, ic) / J;
-        }
       }
   }
   // face normals from the left cell, getrusanov.f90:12-17 and interfaceflux_all.f90:46-76
@@ -421,7 +413,7 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   size_t oRes = P.take<double>(nq), oQvf = P.take<double>(nfp * 9), oFc = P.take<double>(nfp * 8),
          oAzf = P.take<double>(nfp), onQs = P.take<double>((size_t)NC * NS * 18), onQvf = P.take<double>(nfp * 18),
          onAs = P.take<double>((size_t)NC * NS * 2), omet = P.take<double>(nfp * 2),
-         ogco = P.take<double>((size_t)NC * NS * NG), oinvJ = P.take<double>((size_t)NC * NS),
+         oinvJ = P.take<double>((size_t)NC * NS),
          oSe = P.take<double>((size_t)NC * 2), omuf = P.take<double>((size_t)NC * 4), odiag = P.take<double>((size_t)NC * 2),
          of2 = P.take<int4>(f2.size() + 1), of1 = P.take<int2>(f1.size() + 1),
          ofn2 = P.take<FaceNorm>(fn2.size() + 1), ofn1 = P.take<FaceNorm>(fn1.size() + 1),
@@ -461,7 +453,6 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   s.nQvf = (double*)(A + onQvf);
   s.nAs = (double*)(A + onAs);
   s.met = (const double*)(A + omet);
-  s.gco = (const double*)(A + ogco);
   s.invJ = (const double*)(A + oinvJ);
   s.Se = (double*)(A + oSe);
   s.Se6 = s.Se + NC;
@@ -495,7 +486,6 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
     if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->st);
   };
   up((void*)s.met, met.data(), met.size() * sizeof(double));
-  up((void*)s.gco, gco.data(), gco.size() * sizeof(double));
   up((void*)s.invJ, invJ.data(), invJ.size() * sizeof(double));
   up((void*)s.face2, f2.data(), f2.size() * sizeof(int4));
   up((void*)s.face1, f1.data(), f1.size() * sizeof(int2));

@@ -73,7 +73,6 @@ struct SolveDev {
   double* nQvf;
   double* nAs;
   const double* met;
-  const double* gco;
   const double* invJ;
   double* Se;
   double* Se6;                  // the same sum for variable 6 (last stage, when plot_flag is set)
@@ -96,6 +95,7 @@ struct SolveDev {
   double* diag;                 // per-cell diagnostic partial sums [e][2]
   const int* plot_flag;         // nonzero: the last stage records Se6 (read by E1 at run time)
   double* nQs9;                 // [e][sp][2] grad A_z of variable 9 (nablaQs(9,:,...)), kept apart from nQs
+  void* pad3;                   // keeps the size a multiple of 16 bytes
 };
 
 // One RK stage update: Qnew = sum_j c[j]*src[j] + cQ*Q + cR*R (+ cR0*R0), with

@@ -96,7 +96,6 @@ struct D {
   static constexpr int NS = N * N;
   static constexpr int NF1 = (N + 1) * N;
   static constexpr int NFP = 2 * NF1;
-  static constexpr int NG = 4 * (N + 1);  // gradient weights per solution point
 };
 
 // element-local flux-point index of face point nfp (0-based) of local face lf (1..4),
@@ -1028,33 +1027,57 @@ __global__ void __launch_bounds__(256) k_diag_face(SolveDev s) {
   }
 }
 
-// nablaQsp(v0..v1) (compflux.f90:107-157) from the current Qvf, 0-based variables
-template <int N>
-__global__ void __launch_bounds__(256) k_nqsp(SolveDev s, int v0, int v1) {
-  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NG = D<N>::NG;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= s.NC * NS) return;
-  const int c = t / NS, p = t - c * NS, is = p % N, js = p / N;
-  const double* w = s.gco + (size_t)c * NG * NS + p;
-  const double* q = s.Qvf + (size_t)c * NFP * 9;
-  for (int k = v0; k <= v1; k++) {
-    double gx = 0.0, gy = 0.0;
-#pragma unroll
-    for (int r = 0; r <= N; r++) {
-      const double fa = q[(js * (N + 1) + r) * 9 + k], fb = q[(NF1 + r * N + is) * 9 + k];
-      gx += w[r * NS] * fa;
-      gx += w[((N + 1) + r) * NS] * fb;
-      gy += w[(2 * (N + 1) + r) * NS] * fa;
-      gy += w[(3 * (N + 1) + r) * NS] * fb;
-    }
-    if (k < 8) {
-      s.nQs[(size_t)t * 18 + k] = gx;
-      s.nQs[(size_t)t * 18 + 9 + k] = gy;
-    } else {  // variable 9 is kept in its own array (SolveDev::nQs9)
-      s.nQs9[(size_t)t * 2] = gx;
-      s.nQs9[(size_t)t * 2 + 1] = gy;
-    }
+// nablaQsp(v0..v1) (compflux.f90:107-157) from the current Qvf, 0-based variables, for
+// cells [e0, e0+cnt): the conservative form of E2 (metric-state products differentiated
+// along the lines on the integer pipes), 2 (v1-v0+1) line quantities per cell
+template <int N, class O>
+__device__ __forceinline__ void nqsp_cells(const SolveDev& s, int e0, int cnt, int v0, int v1, double* sm) {
+  constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP;
+  const int nv = v1 - v0 + 1, NQ = 2 * nv;
+  double* sP = sm;                  // [cnt][NFP][NQ] Q_k * S_x (k < nv), Q_k * S_y
+  double* sG = sP + cnt * NFP * NQ;  // [cnt][NS][NQ] the xi-line part
+  for (int i = threadIdx.x; i < cnt * NFP * nv; i += blockDim.x) {
+    const int kk = i % nv, lf = i / nv;
+    const size_t g = (size_t)e0 * NFP + lf;
+    const double q = s.Qvf[g * 9 + v0 + kk];
+    sP[lf * NQ + kk] = q * s.met[2 * g];
+    sP[lf * NQ + nv + kk] = q * s.met[2 * g + 1];
   }
+  __syncthreads();
+#pragma unroll 1
+  for (int fam = 0; fam < 2; fam++) {
+    for (int t = threadIdx.x; t < cnt * N * NQ; t += blockDim.x) {
+      const int c = t % NQ, el = t / NQ, le = el / N, ln = el - le * N;
+      const int fp0 = fam ? NF1 + ln : ln * (N + 1), fps = fam ? N : 1;
+      double y[N];
+      deriv_line<N, O>(sP + (le * NFP + fp0) * NQ + c, fps * NQ, y);
+      const int p0 = fam ? ln : ln * N, ps = fam ? N : 1;
+      double* g = sG + (le * NS + p0) * NQ + c;
+      if (!fam) {
+#pragma unroll
+        for (int i = 0; i < N; i++) g[i * ps * NQ] = y[i];
+      } else {
+        const int k = v0 + c % nv, d = c / nv;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+          const size_t gs = (size_t)(e0 + le) * NS + p0 + i * ps;
+          const double a = (g[i * ps * NQ] + y[i]) * s.invJ[gs];
+          if (k < 8) s.nQs[gs * 18 + 9 * d + k] = a;
+          else s.nQs9[gs * 2 + d] = a;  // variable 9 is kept in its own array
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_nqsp(SolveDev s, int epb, int v0, int v1) {
+  extern __shared__ double sm[];
+  const int e0 = blockIdx.x * epb;
+  const int cnt = min(epb, s.NC - e0);
+  if (cnt <= 0) return;
+  nqsp_cells<N, OpsTU>(s, e0, cnt, v0, v1, sm);
 }
 
 // per-cell sum of (dBx/dx + dBy/dy)^2 (iterations.f90:48) into diag[e][1]

@@ -39,6 +39,7 @@ void set_smem_limits() {
   cudaFuncSetAttribute(k_e3<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   cudaFuncSetAttribute(k_ct_elem<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   cudaFuncSetAttribute(k_diag_interp<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(k_nqsp<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (dev < 64) done[dev] = true;
 }
 }  // namespace
@@ -112,8 +113,10 @@ void launch_diag<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int mo
 }
 template <>
 void launch_nqsp<kN>(const SolveDev& s, int v0, int v1, cudaStream_t st) {
-  const int n = s.NC * D<kN>::NS;
-  k_nqsp<kN><<<(n + 255) / 256, 256, 0, st>>>(s, v0, v1);
+  // 4 cells per 128 threads; 12 kB of shared memory per cell for all nine variables
+  const int epb = 4, nq = 2 * (v1 - v0 + 1);
+  const size_t smem = sizeof(double) * epb * (size_t)(D<kN>::NFP + D<kN>::NS) * nq;
+  k_nqsp<kN><<<grid_cells(s.NC, epb), 128, smem, st>>>(s, epb, v0, v1);
 }
 template <>
 void launch_divb<kN>(const SolveDev& s, cudaStream_t st) {
