@@ -137,10 +137,10 @@ Launch default_launch(int N, int which) {
   // which: 0 = E1, 1 = E2, 2 = E3, 3 = CT; cells per CTA and threads per CTA as the
   // autotuner picked them on GB300 for N = 3..6; the CT passes take about 128/(2N) cells
   // so that their (cell, line) loop fills the 128 threads
-  static const int epb[kMaxN + 1][4] = {{0}, {0}, {16, 16, 16, 32}, {16, 8, 2, 21}, {4, 12, 4, 16},
-                                        {4, 4, 5, 12}, {3, 5, 2, 10}, {2, 2, 2, 9}, {2, 2, 2, 8}};
-  static const int thr[kMaxN + 1][4] = {{0}, {0}, {128, 128, 128, 128}, {256, 224, 32, 128}, {64, 512, 96, 128},
-                                        {128, 320, 160, 128}, {96, 480, 128, 128}, {128, 128, 128, 128},
+  static const int epb[kMaxN + 1][4] = {{0}, {0}, {16, 16, 16, 32}, {16, 4, 2, 21}, {4, 4, 4, 16},
+                                        {4, 2, 5, 12}, {3, 2, 2, 10}, {2, 2, 2, 9}, {2, 2, 2, 8}};
+  static const int thr[kMaxN + 1][4] = {{0}, {0}, {128, 128, 128, 128}, {256, 96, 32, 128}, {64, 128, 96, 128},
+                                        {128, 160, 160, 128}, {96, 192, 128, 128}, {128, 128, 128, 128},
                                         {128, 128, 128, 128}};
   return Launch{epb[N][which], thr[N][which]};
 }
