@@ -233,6 +233,8 @@ def run_gpu(args):
     qh = pinned.numpy()
     qh[:] = Q
     e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(max(1, min(args.warmup, 3))):  # untimed: first use of the copy stream and events
+        sol.step_host(qh, qh, 1)
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -382,9 +384,9 @@ def run_serving(args, device, tmp):
 # (2*DFMA + DADD + DMUL); DRAM bytes read + written.  FP64_FORM_... is the count of the
 # same stage with the line operators in FP64 as well (measured the same way before they
 # moved to the integer pipes): the stage's work in FP64-instruction units.
-FP64_PER_ELEMENT_STAGE: dict = {5: (5798, 8128)}
+FP64_PER_ELEMENT_STAGE: dict = {5: (5568, 7898)}
 FP64_FORM_OPS_PER_ELEMENT_STAGE: dict = {5: 10798}
-TRAFFIC_PER_ELEMENT_STAGE: dict = {5: 26344}
+TRAFFIC_PER_ELEMENT_STAGE: dict = {5: 26615}
 
 
 def cpu_baseline(case_dir, dof, warm=1, timed=2):
