@@ -38,13 +38,13 @@ void initial_point(int problem, double gam, double x, double y, const double* B,
 //   Qvf        [e][fp][9]    fp = family-1 points (jfp*(N+1)+ifp), then family-2
 //                            points ((N+1)N + jfp*N+ifp): one block per cell
 //   Fc         [e][fp][8]    inviscid contravariant flux (F1 / G2)
-//   Azf        [e][fp]       A_z at the flux points (upwinded on faces)
-//   nQs        [e][js][is][2][9]
+//   Azf        [e][fp]       A_z at the flux points (upwinded on faces after a stage,
+//                            face-averaged after the CT projection)
+//   nQs        [e][js][is][2][9]   (variable 9 is not stored here: see nQs9)
+//   nQs9       [e][js][is][2]      grad A_z of the CT projection / nablaQsp(9,9)
 //   nQvf       [e][fp][2][9]
 //   nAs        [e][js][is][2]
 //   met        [e][fp][2]    (S1(1,1),S1(1,2)) on family 1, (S2(2,1),S2(2,2)) on 2
-//   gco        [e][4(N+1)][js][is] gradient weights Mmat*S/Jac (x-fam1, x-fam2,
-//                            y-fam1, y-fam2)
 //   invJ       [e][js][is]
 //   Se         [e]           AV sensor sum of variable 1 (the reference's SM_IND(1) is log10 of it)
 //   muf        [e][4]        face-averaged AV viscosity per local face 1..4

@@ -1,24 +1,27 @@
 // kernels.cuh -- stage kernels of the residual-and-time-step path, templated on N.
 //
 // One RK stage (compresid.f90:1-67 + the stage update of iterations.f90:162-217) is
-// five launches, one per grid-wide dependency level of the reference's compflux:
+// four launches, one per grid-wide dependency level of the reference's compflux:
 //   E1  cell pass  Q -> flux-point values (all 2N(N+1) points), interior inviscid
 //                  flux, interior A_z, AV sensor           inviscid_flux_interior,
 //                                                          comp_artificial_viscosity
 //   F1  face pass  Rusanov flux on every face point, upwinded A_z, face-averaged Q,
 //                  max wave speed                          interfaceflux, CYCLOCFLUX,
 //                                                          BCFLUX, getrusanovflux
-//   E2  cell pass  grad Q (vars 1-8) and grad A_z at the solution points, grad Q at
-//                  every flux point                        nablaAsp, nablaQsp,
+//   E2  cell pass  face AV viscosities; grad Q (vars 1-8) at the solution and flux
+//                  points of the cells that carry viscous work
+//                                                          compAVflux, nablaQsp,
 //                                                          nablaQ_interior_FP
-//   F2  face pass  face-averaged grad Q, face AV viscosity interfaceVISflux,
-//                                                          BCVISFLUX, CYCLOCVISFLUX,
-//                                                          compAVflux
-//   E3  cell pass  viscous + AV flux, divergence, A_z advection, RK update
-//                                                          comp_viscous_flux,
+//   E3  cell pass  viscous + AV flux with the face-averaged grad Q traces, divergence,
+//                  grad A_z, A_z advection, RK update      interfaceVISflux,
+//                                                          comp_viscous_flux, nablaAsp,
 //                                                          compresid, RK_S5P3
+// (k_f2 stores the face-averaged grad Q traces only when they are downloaded.)
 // Cell passes stage a block of `epb` cells in shared memory; face passes run one
-// thread per face point.  All arithmetic is FP64.
+// thread per face point.  Values are IEEE doubles throughout; the fixed line operators
+// (Lmat interpolation, Mmat differentiation, which carry no data-dependent
+// coefficients) run as exact integer dot products on the integer pipes (fixdot.cuh),
+// all other arithmetic is FP64.
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
