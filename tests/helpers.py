@@ -37,3 +37,38 @@ def var_slice(arr, nvar, keep):
     """Select variables `keep` (0-based) from a flat array whose fastest index has nvar entries."""
     a = np.asarray(arr).reshape(-1, nvar)
     return a[:, keep]
+
+
+ENTROPY_GAM = 5.0 / 3.0
+
+
+def entropy_wave_case(root, nx, N, cfl, T, jitter=0.0):
+    """A periodic [0, 2pi]^2 case (no AV) with dt = T / steps for the entropy wave below:
+    returns (case dir, steps)."""
+    import math
+    h = 2 * math.pi / nx
+    lam = math.sqrt(2) + math.sqrt(ENTROPY_GAM / 0.8)  # |u| + the largest sound speed
+    steps = max(1, int(math.ceil(T / (cfl * h / (N * lam)))))
+    d = make_case(root, problem="orszag_tang", nx=nx, ny=nx, N=N, jitter=jitter, seed=5, artiv=0, dt=T / steps)
+    return d, steps
+
+
+def entropy_wave_state(X, t=0.0):
+    """rho = 1 + 0.2 sin(x + y - 2t), u = v = 1, p = 1, B = A_z = 0: an exact solution of
+    ideal MHD that the scheme advects unchanged in shape.  X is (points, 2)."""
+    rho = 1 + 0.2 * np.sin(X[:, 0] + X[:, 1] - 2 * t)
+    Q = np.zeros((X.shape[0], 9))
+    Q[:, 0] = rho
+    Q[:, 1] = rho
+    Q[:, 2] = rho
+    Q[:, 4] = 1.0 / (ENTROPY_GAM - 1) + rho
+    return Q
+
+
+def quadrature_l2(values, Jac, Xs):
+    """sqrt(sum J w_i w_j v^2 / sum J w_i w_j) with the interpolatory weights of the
+    solution points."""
+    N = len(Xs)
+    w = np.linalg.solve(np.vander(np.asarray(Xs, np.float64), N, increasing=True).T, 1.0 / np.arange(1, N + 1))
+    wJ = np.asarray(Jac) * np.tile(np.outer(w, w).ravel(), np.asarray(Jac).size // (N * N))
+    return float(np.sqrt((np.asarray(values) ** 2 * wJ).sum() / wJ.sum()))

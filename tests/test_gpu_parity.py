@@ -9,7 +9,7 @@ import pytest
 
 import oracle
 from chorus_mhd import Mesh, Solver, reference_layout_sizes
-from helpers import assert_close, make_case, rel_l2
+from helpers import entropy_wave_case, entropy_wave_state, quadrature_l2, assert_close, make_case, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -124,6 +124,38 @@ def test_drop_in_sequence_matches_oracle(case_root):
         s.correct_B_via_curl_Az()
     assert_close(s.state(), o.array("Q"), RUN_TOL, "drop-in sequence")
     assert s.ctime == pytest.approx(o.getd("ctime"), rel=1e-15)
+
+
+def gpu_entropy_wave_error(case_root, nx, N, cfl, T=0.4, jitter=0.0):
+    d, steps = entropy_wave_case(case_root, nx, N, cfl, T, jitter)
+    m = Mesh(d)
+    s = Solver(m, initial_state=False)
+    X = m.darray("XXsolu").reshape(-1, 2)
+    s.upload(np.ascontiguousarray(entropy_wave_state(X).ravel()))
+    s.iterations(steps)
+    err = s.state().reshape(-1, 9)[:, 0] - entropy_wave_state(X, T)[:, 0]
+    e = quadrature_l2(err, m.darray("Jac"), m.darray("Xs"))
+    s.close()
+    return e
+
+
+@pytest.mark.parametrize("N,cfl,sizes,rate", [(3, 0.2, (8, 16, 32, 64), 2.9), (5, 0.02, (8, 16, 32, 64), 4.8)])
+def test_entropy_wave_converges_at_design_order(case_root, N, cfl, sizes, rate):
+    """Through the C-ABI, the exact advected entropy wave is approached as h^N; on the
+    meshes the oracle finishes quickly the errors equal the oracle's to 1e-8 relative."""
+    import math
+    errs = [gpu_entropy_wave_error(case_root, nx, N, cfl) for nx in sizes]
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(len(errs) - 1)]
+    assert rates[-1] >= rate, (errs, rates)
+    d, steps = entropy_wave_case(case_root, sizes[1], N, cfl, 0.4)
+    o = oracle.Oracle(d, threads=0)
+    X = o.array("XXsolu").reshape(-1, 2)
+    o.array("Q")[:] = entropy_wave_state(X).ravel()
+    for _ in range(steps):
+        o.step()
+    e_o = quadrature_l2(o.array("Q").reshape(-1, 9)[:, 0] - entropy_wave_state(X, 0.4)[:, 0], o.array("Jac"), o.array("Xs"))
+    assert abs(errs[1] - e_o) <= 1e-8 * e_o
+    o.close()
 
 
 @pytest.mark.parametrize("spec", [dict(problem="orszag_tang", nx=6, ny=5, N=4, jitter=0.1, seed=17),

@@ -11,7 +11,9 @@ follow from the reference's own definitions:
   * the unstaggered CT projection keeps the diagnostic div B at round-off on affine
     meshes (iterations.f90:48,67);
   * Orszag-Tang initial data of setinitialcond.f90:16-35;
-  * map invariants of CONNECTIVITY / CONNECT_BDRY / MAPCYCLOC.
+  * map invariants of CONNECTIVITY / CONNECT_BDRY / MAPCYCLOC;
+  * convergence at the design order N of the spectral difference method on an exact
+    smooth solution (an entropy wave), on uniform and curved cells.
 """
 import math
 
@@ -19,7 +21,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import make_case
+from helpers import entropy_wave_case, entropy_wave_state, make_case, quadrature_l2
 
 
 @pytest.mark.parametrize("N", [2, 3, 4, 5, 6, 7, 8, 9, 10])
@@ -148,3 +150,27 @@ def test_restart_round_trip(case_root, tmp_path):
     assert o2.geti("iter") == 2
     raw = open(p, "rb").read()
     assert len(raw) == 4 + 8 + 16 * (4 + 8 * 9 * 9)
+
+
+def entropy_wave_error(case_root, nx, N, cfl, T=0.4, jitter=0.0):
+    d, steps = entropy_wave_case(case_root, nx, N, cfl, T, jitter)
+    o = oracle.Oracle(d, threads=0)
+    X = o.array("XXsolu").reshape(-1, 2)
+    o.array("Q")[:] = entropy_wave_state(X).ravel()
+    for _ in range(steps):
+        o.step()
+    err = o.array("Q").reshape(-1, 9)[:, 0] - entropy_wave_state(X, T)[:, 0]
+    e = quadrature_l2(err, o.array("Jac"), o.array("Xs"))
+    o.close()
+    return e
+
+
+@pytest.mark.parametrize("N,cfl,sizes,rate,jitter", [(3, 0.2, (8, 16, 32), 2.7, 0.0), (5, 0.02, (8, 16), 4.5, 0.0),
+                                                     (4, 0.05, (8, 16), 3.5, 0.1)])
+def test_entropy_wave_converges_at_design_order(case_root, N, cfl, sizes, rate, jitter):
+    """The L2 error of rho against the exact advected wave falls as h^N (the method's order
+    p+1 = N) under mesh refinement: a pin of the whole residual (interpolation, fluxes,
+    Riemann solver, divergence, metrics, RK) that no single known answer gives."""
+    errs = [entropy_wave_error(case_root, nx, N, cfl, jitter=jitter) for nx in sizes]
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(len(errs) - 1)]
+    assert rates[-1] >= rate, (errs, rates)
