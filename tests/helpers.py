@@ -72,3 +72,22 @@ def quadrature_l2(values, Jac, Xs):
     w = np.linalg.solve(np.vander(np.asarray(Xs, np.float64), N, increasing=True).T, 1.0 / np.arange(1, N + 1))
     wJ = np.asarray(Jac) * np.tile(np.outer(w, w).ravel(), np.asarray(Jac).size // (N * N))
     return float(np.sqrt((np.asarray(values) ** 2 * wJ).sum() / wJ.sum()))
+
+
+def alfven_wave_case(root, nx, N, cfl, T, jitter=0.0):
+    """The circularly polarised Alfven wave case (no AV): returns (case dir, steps).  The
+    wave of amplitude 0.1 on rho = 1, p = 0.1, B_par = 1 moves at the Alfven speed 1 along
+    -(cos 30, sin 30) without change of shape (an exact solution of ideal MHD)."""
+    import math
+    lam = 1.0 + math.sqrt(5.0 / 3 * 0.1 + 1.01) + 0.2
+    h = (1.0 / math.cos(math.radians(30.0))) / nx
+    steps = max(1, int(math.ceil(T / (cfl * h / (N * lam)))))
+    d = make_case(root, problem="alfven", nx=nx, ny=nx, N=N, jitter=jitter, seed=5, artiv=0, dt=T / steps)
+    return d, steps
+
+
+def alfven_wave_bz(X, t):
+    """B_z of the exact wave at time t."""
+    import math
+    xp = X[:, 0] * math.sqrt(3.0) / 2 + X[:, 1] * 0.5
+    return 0.1 * np.cos(2 * math.pi * (xp + t))

@@ -9,7 +9,7 @@ import pytest
 
 import oracle
 from chorus_mhd import Mesh, Solver, reference_layout_sizes
-from helpers import entropy_wave_case, entropy_wave_state, quadrature_l2, assert_close, make_case, rel_l2
+from helpers import alfven_wave_bz, alfven_wave_case, entropy_wave_case, entropy_wave_state, quadrature_l2, assert_close, make_case, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -154,6 +154,32 @@ def test_entropy_wave_converges_at_design_order(case_root, N, cfl, sizes, rate):
     for _ in range(steps):
         o.step()
     e_o = quadrature_l2(o.array("Q").reshape(-1, 9)[:, 0] - entropy_wave_state(X, 0.4)[:, 0], o.array("Jac"), o.array("Xs"))
+    assert abs(errs[1] - e_o) <= 1e-8 * e_o
+    o.close()
+
+
+def test_alfven_wave_converges_at_design_order(case_root):
+    """The circularly polarised Alfven wave through the C-ABI (N = 4, 8^2..64^2): B_z after
+    t = 0.25 approaches the exact wave as h^4, and on 16^2 equals the oracle's error to 1e-8."""
+    import math
+    errs = []
+    for nx in (8, 16, 32, 64):
+        d, steps = alfven_wave_case(case_root, nx, 4, 0.05, 0.25)
+        m = Mesh(d)
+        s = Solver(m)
+        X = m.darray("XXsolu").reshape(-1, 2)
+        s.iterations(steps)
+        errs.append(quadrature_l2(s.state().reshape(-1, 9)[:, 7] - alfven_wave_bz(X, 0.25), m.darray("Jac"),
+                                  m.darray("Xs")))
+        s.close()
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(len(errs) - 1)]
+    assert rates[-1] >= 3.7, (errs, rates)  # RK3 time error enters at the finest mesh
+    d, steps = alfven_wave_case(case_root, 16, 4, 0.05, 0.25)
+    o = oracle.Oracle(d, threads=0)
+    X = o.array("XXsolu").reshape(-1, 2)
+    for _ in range(steps):
+        o.step()
+    e_o = quadrature_l2(o.array("Q").reshape(-1, 9)[:, 7] - alfven_wave_bz(X, 0.25), o.array("Jac"), o.array("Xs"))
     assert abs(errs[1] - e_o) <= 1e-8 * e_o
     o.close()
 

@@ -12,8 +12,9 @@ follow from the reference's own definitions:
     meshes (iterations.f90:48,67);
   * Orszag-Tang initial data of setinitialcond.f90:16-35;
   * map invariants of CONNECTIVITY / CONNECT_BDRY / MAPCYCLOC;
-  * convergence at the design order N of the spectral difference method on an exact
-    smooth solution (an entropy wave), on uniform and curved cells.
+  * convergence at the design order N of the spectral difference method on exact smooth
+    solutions: an entropy wave (hydrodynamics, uniform and curved cells) and a circularly
+    polarised Alfven wave (the magnetic terms, A_z and the CT projection).
 """
 import math
 
@@ -21,7 +22,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import entropy_wave_case, entropy_wave_state, make_case, quadrature_l2
+from helpers import alfven_wave_bz, alfven_wave_case, entropy_wave_case, entropy_wave_state, make_case, quadrature_l2
 
 
 @pytest.mark.parametrize("N", [2, 3, 4, 5, 6, 7, 8, 9, 10])
@@ -172,5 +173,24 @@ def test_entropy_wave_converges_at_design_order(case_root, N, cfl, sizes, rate, 
     p+1 = N) under mesh refinement: a pin of the whole residual (interpolation, fluxes,
     Riemann solver, divergence, metrics, RK) that no single known answer gives."""
     errs = [entropy_wave_error(case_root, nx, N, cfl, jitter=jitter) for nx in sizes]
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(len(errs) - 1)]
+    assert rates[-1] >= rate, (errs, rates)
+
+
+@pytest.mark.parametrize("N,cfl,sizes,rate", [(3, 0.2, (8, 16, 32), 2.75), (4, 0.05, (4, 8, 16), 4.0)])
+def test_alfven_wave_converges_at_design_order(case_root, N, cfl, sizes, rate):
+    """B_z of the circularly polarised Alfven wave after t = 0.25 against the exact wave:
+    the error falls as h^N, pinning the Lorentz force, the induction through A_z and the CT
+    projection (on the background-field extension of A_z)."""
+    errs = []
+    for nx in sizes:
+        d, steps = alfven_wave_case(case_root, nx, N, cfl, 0.25)
+        o = oracle.Oracle(d, threads=0)
+        X = o.array("XXsolu").reshape(-1, 2)
+        for _ in range(steps):
+            o.step()
+        errs.append(quadrature_l2(o.array("Q").reshape(-1, 9)[:, 7] - alfven_wave_bz(X, 0.25), o.array("Jac"),
+                                  o.array("Xs")))
+        o.close()
     rates = [math.log2(errs[i] / errs[i + 1]) for i in range(len(errs) - 1)]
     assert rates[-1] >= rate, (errs, rates)
