@@ -91,3 +91,27 @@ def alfven_wave_bz(X, t):
     import math
     xp = X[:, 0] * math.sqrt(3.0) / 2 + X[:, 1] * 0.5
     return 0.1 * np.cos(2 * math.pi * (xp + t))
+
+
+def diffusion_wave_case(root, nx, N, kind, coef, T, A=1e-3, cfl=0.05):
+    """A small shear wave v = A sin(x) (kind "viscous", mu = coef) or magnetic wave
+    B_z = A sin(x) (kind "resistive", eta0 = coef) on rho = 1, p = 1 at rest: both decay as
+    exp(-coef t) (the heating and magnetic pressure they cause enter at A^2).  Returns
+    (case dir, steps, Q0 builder, variable index)."""
+    import math
+    h = 2 * math.pi / nx
+    lam = math.sqrt(ENTROPY_GAM) + A
+    dt0 = min(cfl * h / (N * lam), 0.05 * (h / N) ** 2 / coef)
+    steps = int(math.ceil(T / dt0))
+    kw = dict(mu=coef) if kind == "viscous" else dict(eta0=coef)
+    d = make_case(root, problem="orszag_tang", nx=nx, ny=nx, N=N, artiv=0, dt=T / steps, **kw)
+    var = 2 if kind == "viscous" else 7
+
+    def state(X, t=0.0):
+        Q = np.zeros((X.shape[0], 9))
+        Q[:, 0] = 1.0
+        Q[:, var] = A * np.sin(X[:, 0]) * math.exp(-coef * t)
+        Q[:, 4] = 1.0 / (ENTROPY_GAM - 1) + 0.5 * Q[:, var] ** 2
+        return Q
+
+    return d, steps, state, var

@@ -9,7 +9,7 @@ import pytest
 
 import oracle
 from chorus_mhd import Mesh, Solver, reference_layout_sizes
-from helpers import alfven_wave_bz, alfven_wave_case, entropy_wave_case, entropy_wave_state, quadrature_l2, assert_close, make_case, rel_l2
+from helpers import alfven_wave_bz, alfven_wave_case, diffusion_wave_case, entropy_wave_case, entropy_wave_state, quadrature_l2, assert_close, make_case, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -154,6 +154,35 @@ def test_entropy_wave_converges_at_design_order(case_root, N, cfl, sizes, rate):
     for _ in range(steps):
         o.step()
     e_o = quadrature_l2(o.array("Q").reshape(-1, 9)[:, 0] - entropy_wave_state(X, 0.4)[:, 0], o.array("Jac"), o.array("Xs"))
+    assert abs(errs[1] - e_o) <= 1e-8 * e_o
+    o.close()
+
+
+@pytest.mark.parametrize("kind", ["viscous", "resistive"])
+def test_diffusion_waves_decay_at_the_exact_rate(case_root, kind):
+    """The viscous shear and resistive magnetic waves through the C-ABI (N = 4, 8^2..32^2):
+    the error against A sin(x) exp(-0.05 t) falls as h^4 and equals the oracle's on 16^2."""
+    import math
+    errs = []
+    for nx in (8, 16, 32):
+        d, steps, state, var = diffusion_wave_case(case_root, nx, 4, kind, 0.05, 0.5)
+        m = Mesh(d)
+        s = Solver(m, initial_state=False)
+        X = m.darray("XXsolu").reshape(-1, 2)
+        s.upload(np.ascontiguousarray(state(X).ravel()))
+        s.iterations(steps)
+        err = s.state().reshape(-1, 9)[:, var] - state(X, 0.5)[:, var]
+        errs.append(quadrature_l2(err, m.darray("Jac"), m.darray("Xs")) / 1e-3)
+        s.close()
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(len(errs) - 1)]
+    assert rates[-1] >= 3.5, (errs, rates)
+    d, steps, state, var = diffusion_wave_case(case_root, 16, 4, kind, 0.05, 0.5)
+    o = oracle.Oracle(d, threads=0)
+    X = o.array("XXsolu").reshape(-1, 2)
+    o.array("Q")[:] = state(X).ravel()
+    for _ in range(steps):
+        o.step()
+    e_o = quadrature_l2(o.array("Q").reshape(-1, 9)[:, var] - state(X, 0.5)[:, var], o.array("Jac"), o.array("Xs")) / 1e-3
     assert abs(errs[1] - e_o) <= 1e-8 * e_o
     o.close()
 

@@ -14,7 +14,9 @@ follow from the reference's own definitions:
   * map invariants of CONNECTIVITY / CONNECT_BDRY / MAPCYCLOC;
   * convergence at the design order N of the spectral difference method on exact smooth
     solutions: an entropy wave (hydrodynamics, uniform and curved cells) and a circularly
-    polarised Alfven wave (the magnetic terms, A_z and the CT projection).
+    polarised Alfven wave (the magnetic terms, A_z and the CT projection), and the
+    decay of small viscous shear and resistive magnetic waves (the viscous and resistive
+    fluxes with their gradients and face traces).
 """
 import math
 
@@ -22,7 +24,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import alfven_wave_bz, alfven_wave_case, entropy_wave_case, entropy_wave_state, make_case, quadrature_l2
+from helpers import alfven_wave_bz, alfven_wave_case, diffusion_wave_case, entropy_wave_case, entropy_wave_state, make_case, quadrature_l2
 
 
 @pytest.mark.parametrize("N", [2, 3, 4, 5, 6, 7, 8, 9, 10])
@@ -194,3 +196,22 @@ def test_alfven_wave_converges_at_design_order(case_root, N, cfl, sizes, rate):
         o.close()
     rates = [math.log2(errs[i] / errs[i + 1]) for i in range(len(errs) - 1)]
     assert rates[-1] >= rate, (errs, rates)
+
+
+@pytest.mark.parametrize("kind", ["viscous", "resistive"])
+def test_diffusion_waves_decay_at_the_exact_rate(case_root, kind):
+    """v = A sin(x) with viscosity mu, B_z = A sin(x) with resistivity eta0: after t = 0.5
+    the wave equals A sin(x) exp(-0.05 t) to an error falling as h^N (N = 4)."""
+    errs = []
+    for nx in (4, 8, 16):
+        d, steps, state, var = diffusion_wave_case(case_root, nx, 4, kind, 0.05, 0.5)
+        o = oracle.Oracle(d, threads=0)
+        X = o.array("XXsolu").reshape(-1, 2)
+        o.array("Q")[:] = state(X).ravel()
+        for _ in range(steps):
+            o.step()
+        err = o.array("Q").reshape(-1, 9)[:, var] - state(X, 0.5)[:, var]
+        errs.append(quadrature_l2(err, o.array("Jac"), o.array("Xs")) / 1e-3)
+        o.close()
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(len(errs) - 1)]
+    assert rates[-1] >= 3.5 and errs[-1] < 1e-5, (errs, rates)
