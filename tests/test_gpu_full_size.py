@@ -123,3 +123,15 @@ def test_full_size_host_step_equals_resident_steps(mesh):
     b.close()
     assert np.array_equal(qa, qout)
     assert [r["residglob"] for r in diag] == [r["residglob"] for r in ref_diag]
+
+
+def test_full_size_free_stream_is_preserved(mesh):
+    """A uniform state on the jittered 512x512 mesh has a zero residual to round-off."""
+    s = Solver(mesh, initial_state=False)
+    q0 = np.array([1.3, 0.4, -0.2, 0.1, 5.0, 0.7, -0.3, 0.2, 0.0])
+    s.upload(np.ascontiguousarray(np.tile(q0, s.nq // 9)))
+    s.compresid()
+    from chorus_mhd import reference_layout_sizes
+    r = s.array("resid", reference_layout_sizes(s.N, s.ncell)["resid"])
+    assert np.abs(r).max() < 1e-10
+    s.close()
