@@ -189,7 +189,7 @@ size_t cell_smem_bytes(int N, int epb, int pass) {
     case 0: d = (size_t)epb * (NS * 9 + 2 * NS + NFP * 9) + N * N; break;
     case 1: d = (size_t)epb * (NFP * 16 + NS * 17); break;
     case 2: d = (size_t)epb * (NFP * 8 + NS * (1 + 9 + 1 + 2) + NFP * 2); break;
-    default: d = (size_t)epb * NFP * 2; break;
+    default: d = (size_t)epb * (NFP * 2 + NS * 2); break;
   }
   return sizeof(double) * d;
 }

@@ -868,7 +868,7 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
     double* sA = sm;  // [epb][NS] A_z at the solution points
     for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sA[i] = s.Q[((size_t)e0 * NS + i) * 9 + 8];
     __syncthreads();
-    // one (cell, line) per thread, the mirror symmetry of the points as in E1
+    // one (cell, line) per thread, the line operator on the integer pipes as in E1
     for (int t = threadIdx.x; t < cnt * 2 * N; t += blockDim.x) {
       const int e = t / (2 * N), line = t - e * 2 * N;
       const bool fam1 = line < N;
@@ -876,35 +876,21 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
       const double* qb = sA + e * NS + (fam1 ? ln * N : ln);
       const int qs = fam1 ? 1 : N;
       const int f0 = fam1 ? ln * (N + 1) : NF1 + ln, fs = fam1 ? 1 : N;
-      const size_t g0 = (size_t)(e0 + e) * NFP;
-      double v[N];
+      double v[N], y[N + 1];
 #pragma unroll
       for (int sp = 0; sp < N; sp++) v[sp] = qb[sp * qs];
-      double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
+      interp_line<N, O>(v, y);
+      double* az = s.Azf + (size_t)(e0 + e) * NFP + f0;
 #pragma unroll
-      for (int j = 0; j < N / 2; j++) {
-        ev[j] = v[j] + v[N - 1 - j];
-        od[j] = v[j] - v[N - 1 - j];
-      }
-#pragma unroll
-      for (int f = 0; f <= N / 2; f++) {
-        double E = (N & 1) ? O::ops().LMID[f] * v[(N - 1) / 2] : 0.0;
-        double Od = 0.0;
-#pragma unroll
-        for (int j = 0; j < N / 2; j++) {
-          E += O::ops().CE[f * kHalfS + j] * ev[j];
-          Od += O::ops().CO[f * kHalfS + j] * od[j];
-        }
-        const size_t ga = g0 + f0 + f * fs, gb = g0 + f0 + (N - f) * fs;
-        s.Azf[ga] = E + Od;
-        if (f != N - f) s.Azf[gb] = E - Od;
-      }
+      for (int f = 0; f <= N; f++) az[f * fs] = y[f];
     }
   } else {
     // nablaQsp(9,9) (compflux.f90:107-157): (1/J) sum_r Mmat (A_z S) over both line
-    // families, one (cell, point, component) per thread; then update_B
+    // families, each component differentiated along its lines on the integer pipes, one
+    // (cell, line, component) per thread, the xi lines first; then update_B
     // (magnetic_potential.f90:44-67): B = B0 + curl A_z
-    double* sZ = sm;  // [epb][NFP][2] A_z * (S_x, S_y)
+    double* sZ = sm;                  // [epb][NFP][2] A_z * (S_x, S_y)
+    double* sP = sZ + epb * NFP * 2;  // [epb][NS][2]  the xi-line part of the gradient
     for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
       const size_t g = (size_t)e0 * NFP + i;
       const double z = s.Azf[g];
@@ -912,20 +898,29 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
       sZ[2 * i + 1] = z * s.met[2 * g + 1];
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < cnt * NS * 2; t += blockDim.x) {
-      const int c = t & 1, ep = t >> 1, e = ep / NS, p = ep - e * NS, is = p % N, js = p / N;
-      const double* az = sZ + e * NFP * 2 + c;
-      double a = 0.0;
+#pragma unroll 1
+    for (int fam = 0; fam < 2; fam++) {
+      for (int t = threadIdx.x; t < cnt * N * 2; t += blockDim.x) {
+        const int c = t & 1, el = t >> 1, e = el / N, ln = el - e * N;
+        const int fp0 = fam ? NF1 + ln : ln * (N + 1), fps = fam ? N : 1;
+        double y[N];
+        deriv_line<N, O>(sZ + (e * NFP + fp0) * 2 + c, fps * 2, y);
+        const int p0 = e * NS + (fam ? ln : ln * N), ps = fam ? N : 1;
+        if (!fam) {
 #pragma unroll
-      for (int r = 0; r <= N; r++) {
-        a += O::ops().M[r + (N + 1) * is] * az[(js * (N + 1) + r) * 2];
-        a += O::ops().M[r + (N + 1) * js] * az[(NF1 + r * N + is) * 2];
+          for (int i = 0; i < N; i++) sP[(p0 + i * ps) * 2 + c] = y[i];
+        } else {
+#pragma unroll
+          for (int i = 0; i < N; i++) {
+            const size_t gs = (size_t)e0 * NS + p0 + i * ps;
+            const double a = (sP[(p0 + i * ps) * 2 + c] + y[i]) * s.invJ[gs];
+            s.nQs9[gs * 2 + c] = a;
+            if (c) s.Q[gs * 9 + 5] = a + s.B0x;  // Bx = dA/dy
+            else s.Q[gs * 9 + 6] = s.B0y - a;    // By = -dA/dx
+          }
+        }
       }
-      const size_t gs = (size_t)e0 * NS + ep;
-      a *= s.invJ[gs];
-      s.nQs9[gs * 2 + c] = a;
-      if (c) s.Q[gs * 9 + 5] = a + s.B0x;    // Bx = dA/dy
-      else s.Q[gs * 9 + 6] = -a + s.B0y;     // By = -dA/dx
+      __syncthreads();
     }
   }
 }

@@ -21,7 +21,7 @@ inline size_t smem_e2(int epb) {
 inline size_t smem_e3(int epb) {
   return sizeof(double) * ((size_t)epb * (D<kN>::NFP * 8 + D<kN>::NS * (1 + 9 + 1 + 2) + D<kN>::NFP * 2));
 }
-inline size_t smem_ct(int epb) { return sizeof(double) * epb * D<kN>::NFP * 2; }
+inline size_t smem_ct(int epb) { return sizeof(double) * epb * (D<kN>::NFP * 2 + D<kN>::NS * 2); }
 inline int grid_cells(int nc, int epb) { return (nc + epb - 1) / epb; }
 
 // threads per CTA of a face-point pass: 256, or 64 when that leaves fewer than about
