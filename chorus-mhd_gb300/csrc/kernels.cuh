@@ -975,27 +975,12 @@ __device__ __forceinline__ void diag_interp_body(const SolveDev& s, int e0, int 
     const int qs = fam1 ? 2 : 2 * N;
     const int f0 = fam1 ? ln * (N + 1) : NF1 + ln, fs = fam1 ? 1 : N;
     double* ob = s.Qvf + ((size_t)(e0 + e) * NFP + f0) * 9 + 5 + v;
-    double w[N];
+    double w[N], y[N + 1];
 #pragma unroll
     for (int sp = 0; sp < N; sp++) w[sp] = qb[sp * qs];
-    double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
+    interp_line<N, O>(w, y);
 #pragma unroll
-    for (int j = 0; j < N / 2; j++) {
-      ev[j] = w[j] + w[N - 1 - j];
-      od[j] = w[j] - w[N - 1 - j];
-    }
-#pragma unroll
-    for (int f = 0; f <= N / 2; f++) {
-      double E = (N & 1) ? O::ops().LMID[f] * w[(N - 1) / 2] : 0.0;
-      double Od = 0.0;
-#pragma unroll
-      for (int j = 0; j < N / 2; j++) {
-        E += O::ops().CE[f * kHalfS + j] * ev[j];
-        Od += O::ops().CO[f * kHalfS + j] * od[j];
-      }
-      ob[(size_t)f * fs * 9] = E + Od;
-      if (f != N - f) ob[(size_t)(N - f) * fs * 9] = E - Od;
-    }
+    for (int f = 0; f <= N; f++) ob[(size_t)f * fs * 9] = y[f];
   }
 }
 
