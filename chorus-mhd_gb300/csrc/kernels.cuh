@@ -694,15 +694,19 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
     // contiguous block copies (coalesced), issued together so their latencies overlap;
     // the state itself is read where it is used (the update is elementwise over the
     // block's contiguous state)
-    const double* fi = s.Fc + (size_t)e0 * NFP * 8;
+    // (16-byte loads: Fc's per-cell block and each metric pair are 16-byte aligned)
+    const double2* fi = reinterpret_cast<const double2*>(s.Fc + (size_t)e0 * NFP * 8);
+    double2* sF2 = reinterpret_cast<double2*>(sF);
 #pragma unroll 4
-    for (int i = threadIdx.x; i < cnt * NFP * 8; i += blockDim.x) sF[i] = fi[i];
+    for (int i = threadIdx.x; i < cnt * NFP * 4; i += blockDim.x) sF2[i] = fi[i];
     for (int i = threadIdx.x; i < cnt * NS; i += blockDim.x) sJ[i] = s.invJ[(size_t)e0 * NS + i];
+    const double2* met2 = reinterpret_cast<const double2*>(s.met);
     for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
       const size_t g = (size_t)e0 * NFP + i;
       const double z = s.Azf[g];
-      sZ[2 * i] = z * s.met[2 * g];
-      sZ[2 * i + 1] = z * s.met[2 * g + 1];
+      const double2 m = met2[g];
+      sZ[2 * i] = z * m.x;
+      sZ[2 * i + 1] = z * m.y;
     }
   }
   __syncthreads();
