@@ -171,6 +171,20 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// dst[0..n) = src[0..n) by the whole CTA, in 16-byte pieces when both are 16-byte
+// aligned (the branch is uniform over the CTA)
+__device__ __forceinline__ void block_copy(double* dst, const double* src, int n) {
+  if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+    const double2* s2 = reinterpret_cast<const double2*>(src);
+    double2* d2 = reinterpret_cast<double2*>(dst);
+#pragma unroll 4
+    for (int i = threadIdx.x; i < (n >> 1); i += blockDim.x) d2[i] = s2[i];
+    if ((n & 1) && threadIdx.x == 0) dst[n - 1] = src[n - 1];
+  } else {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  }
+}
+
 // element-local flux-point index of the i-th interior flux point (i < 2N(N-1)):
 // family 1 with ifp = 1..N-1, then family 2 with jfp = 1..N-1
 template <int N>
@@ -251,17 +265,14 @@ __device__ __forceinline__ void deriv_line(const double* x, int xs, double (&y)[
 template <int N, class O>
 __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int epb, int sensor, double* sm) {
   constexpr int NS = D<N>::NS, NF1 = D<N>::NF1, NFP = D<N>::NFP, NINT = 2 * N * (N - 1);
-  double* sQ = sm;                    // [epb][NS][9]   cell states
+  double* sQ = sm;                    // [epb][NS][9]   cell states (16-byte aligned)
   double* sT = sQ + epb * NS * 9;     // [epb][NS]      sensor scratch
   double* sU = sT + epb * NS;         // [epb][NS]
   double* sV = sU + epb * NS;         // [epb][NFP][9]  flux-point values
   double* sA = sV + epb * NFP * 9;    // AV smoothing operator (N, N)
-  {
-    // all global traffic of the pass is contiguous block copies (coalesced)
-    const double* g = s.Q + (size_t)e0 * NS * 9;
-    for (int i = threadIdx.x; i < cnt * NS * 9; i += blockDim.x) sQ[i] = g[i];
-    for (int i = threadIdx.x; i < N * N; i += blockDim.x) sA[i] = O::ops().A[i];
-  }
+  // all global traffic of the pass is contiguous block copies (coalesced)
+  block_copy(sQ, s.Q + (size_t)e0 * NS * 9, cnt * NS * 9);
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) sA[i] = O::ops().A[i];
   __syncthreads();
   // interpolation to every flux point, one (cell, line, variable) per thread so that
   // every lane of every warp does work; the line operator runs on the integer pipes,
@@ -301,8 +312,7 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
     s.Azf[g] = qf[8];
   }
   {
-    double* gv = s.Qvf + (size_t)e0 * NFP * 9;
-    for (int i = threadIdx.x; i < cnt * NFP * 9; i += blockDim.x) gv[i] = sV[i];
+    block_copy(s.Qvf + (size_t)e0 * NFP * 9, sV, cnt * NFP * 9);
   }
   if (!sensor) {
     if (s.skip)
