@@ -104,7 +104,7 @@ __device__ __forceinline__ void for_each_tile(int* counter, int nt, const int4* 
 // multi-order bodies need more registers than any single order; E1 and E3 are held to
 // 64 (4 and 8 CTAs per SM), which measured faster than fewer CTAs without spills
 __global__ void __launch_bounds__(256, 4) kb_e1(BatchDev b, int slot, int sensor_on) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[0], b.ctiles, b.solves, [&](const int4& T, const SolveDev& s) {
     if (T.y == 0 && threadIdx.x == 0) *s.eig = 0ull;  // the solve's stage starts its wave-speed maximum
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(256, 4) kb_e1(BatchDev b, int slot, int sensor
 }
 
 __global__ void __launch_bounds__(256) kb_e2(BatchDev b, int slot) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[2], b.ctiles + b.ntiles[0], b.solves,
                 [&](const int4& T, const SolveDev& s) {
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256) kb_e2(BatchDev b, int slot) {
 }
 
 __global__ void __launch_bounds__(128, 8) kb_e3(BatchDev b, int slot, int stage) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[3], b.ctiles + b.ntiles[0] + b.ntiles[2], b.solves,
                 [&](const int4& T, const SolveDev& s) {
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(128, 8) kb_e3(BatchDev b, int slot, int stage)
 }
 
 __global__ void __launch_bounds__(128) kb_ct(BatchDev b, int slot, int mode) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   pdl_wait();
   for_each_tile(b.counters + slot, b.ntiles[4], b.ctiles + b.ntiles[0] + b.ntiles[2] + b.ntiles[3], b.solves,
                 [&](const int4& T, const SolveDev& s) {

@@ -393,7 +393,7 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
 // cells [c0, c1) of the solve, epb per CTA
 template <int N>
 __global__ void __launch_bounds__(512) k_e1(SolveDev s, int epb, int sensor, int c0, int c1) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   pdl_wait();
   // bit 4: the first pass of a stage, which starts the stage's wave-speed maximum
   if ((sensor & 4) && c0 == 0 && blockIdx.x == 0 && threadIdx.x == 0) *s.eig = 0ull;
@@ -633,7 +633,7 @@ __device__ __forceinline__ bool needs_gradients(const SolveDev& s, int c) {
 // them in groups of epb, so chunks without viscous work cost one coalesced test
 template <int N>
 __global__ void __launch_bounds__(512) k_e2(SolveDev s, int epb, int chunk) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   pdl_wait();
   __shared__ int list[512];
   __shared__ int woff[17];
@@ -858,7 +858,7 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
 
 template <int N>
 __global__ void __launch_bounds__(512) k_e3(SolveDev s, RKStage rk, int epb, int update) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   pdl_wait();
   const int e0 = blockIdx.x * epb;
   const int cnt = min(epb, s.NC - e0);
@@ -941,7 +941,7 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
 
 template <int N>
 __global__ void __launch_bounds__(256) k_ct_elem(SolveDev s, int epb, int mode, int c0, int c1) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   pdl_wait();
   const int e0 = c0 + blockIdx.x * epb;
   const int cnt = min(epb, c1 - e0);
@@ -1000,7 +1000,7 @@ __device__ __forceinline__ void diag_interp_body(const SolveDev& s, int e0, int 
 
 template <int N>
 __global__ void __launch_bounds__(256) k_diag_interp(SolveDev s, int epb) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   const int e0 = blockIdx.x * epb;
   const int cnt = min(epb, s.NC - e0);
   if (cnt <= 0) return;
@@ -1070,7 +1070,7 @@ __device__ __forceinline__ void nqsp_cells(const SolveDev& s, int e0, int cnt, i
 
 template <int N>
 __global__ void __launch_bounds__(256) k_nqsp(SolveDev s, int epb, int v0, int v1) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   const int e0 = blockIdx.x * epb;
   const int cnt = min(epb, s.NC - e0);
   if (cnt <= 0) return;
