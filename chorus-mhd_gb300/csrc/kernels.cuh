@@ -303,12 +303,12 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
     const int e = t / NINT, fp = interior_fp<N>(t - e * NINT);
     const double* qf = sV + (e * NFP + fp) * 9;
     const size_t g = (size_t)(e0 + e) * NFP + fp;
-    const double sx = s.met[2 * g], sy = s.met[2 * g + 1];
+    const double2 m = reinterpret_cast<const double2*>(s.met)[g];  // 16-byte metric pair
     double F[8];
-    iflux_contra(qf, sx, sy, gm1, F);
-    double* fo = s.Fc + g * 8;
+    iflux_contra(qf, m.x, m.y, gm1, F);
+    double2* fo = reinterpret_cast<double2*>(s.Fc + g * 8);  // 64-byte flux record
 #pragma unroll
-    for (int k = 0; k < 8; k++) fo[k] = F[k];
+    for (int k = 0; k < 4; k++) fo[k] = make_double2(F[2 * k], F[2 * k + 1]);
     s.Azf[g] = qf[8];
   }
   {
