@@ -482,9 +482,9 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
     rusanov_core(ql, qr, fn.ux, fn.uy, s.gam, fn.msl, Fh, vnl, ev);
     evb = ev_bits(ev, s.err);
     const double az = vnl > 0.0 ? ql[8] : qr[8];
-    double* fl = s.Fc + gl * 8;
+    double2* fl = reinterpret_cast<double2*>(s.Fc + gl * 8);  // 64-byte flux records
 #pragma unroll
-    for (int k = 0; k < 8; k++) fl[k] = Fh[k];
+    for (int k = 0; k < 4; k++) fl[k] = make_double2(Fh[2 * k], Fh[2 * k + 1]);
     s.Azf[gl] = az;
     if (two && s.skip && nfp == 0) {
       const int4 fc = s.face2[f];
@@ -494,9 +494,9 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
       }
     }
     if (two) {
-      double* fr = s.Fc + gr * 8;
+      double2* fr = reinterpret_cast<double2*>(s.Fc + gr * 8);
 #pragma unroll
-      for (int k = 0; k < 8; k++) fr[k] = times_sign(Fh[k], fn.ss);
+      for (int k = 0; k < 4; k++) fr[k] = make_double2(times_sign(Fh[2 * k], fn.ss), times_sign(Fh[2 * k + 1], fn.ss));
       s.Azf[gr] = az;
       double* al = s.Qvf + gl * 9;
       double* ar = s.Qvf + gr * 9;
@@ -908,8 +908,9 @@ __device__ __forceinline__ void ct_elem_body(const SolveDev& s, int e0, int cnt,
     for (int i = threadIdx.x; i < cnt * NFP; i += blockDim.x) {
       const size_t g = (size_t)e0 * NFP + i;
       const double z = s.Azf[g];
-      sZ[2 * i] = z * s.met[2 * g];
-      sZ[2 * i + 1] = z * s.met[2 * g + 1];
+      const double2 m = reinterpret_cast<const double2*>(s.met)[g];
+      sZ[2 * i] = z * m.x;
+      sZ[2 * i + 1] = z * m.y;
     }
     __syncthreads();
 #pragma unroll 1
