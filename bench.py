@@ -386,7 +386,7 @@ def run_serving(args, device, tmp):
 # moved to the integer pipes): the stage's work in FP64-instruction units.
 FP64_PER_ELEMENT_STAGE: dict = {5: (5568, 7898)}
 FP64_FORM_OPS_PER_ELEMENT_STAGE: dict = {5: 10798}
-TRAFFIC_PER_ELEMENT_STAGE: dict = {5: 26615}
+TRAFFIC_PER_ELEMENT_STAGE: dict = {5: 26541}
 
 
 def cpu_baseline(case_dir, dof, warm=1, timed=2):
