@@ -103,10 +103,16 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once the sampler is producing (nvidia-smi takes a
+            # moment to start); at most two seconds
+            t_end = time.time() + 2.0
+            while not self.lines and time.time() < t_end and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.lines.clear()
         except Exception:
             self.proc = None
         return self
@@ -428,8 +434,8 @@ def run_reference(args):
         o.step()
         t_est = time.perf_counter() - t0
     k = args.steps
-    if t_est and t_est * k > 150:
-        k = max(1, int(150 / t_est))
+    if t_est and t_est * k > 90:
+        k = max(1, int(90 / t_est))
     t0 = time.perf_counter()
     for _ in range(k):
         o.step()
@@ -456,7 +462,7 @@ def main():
                     help="C2: Orszag-Tang 512^2 jittered N=5 (default); C1: Orszag-Tang 64^2 N=4; "
                          "C3: rotor 256^2 jittered N=4, FREE boundaries")
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="chorus", choices=["chorus", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
