@@ -25,3 +25,27 @@ def test_reference_arm_prints_the_contract_line():
     assert b["cpu_baseline"]["kind"] in ("port", "reference")
     assert b["e2e"]["value"] == b["value"] and b["e2e"]["h2d_bytes_per_step"] == 0
     assert "workload" in b["config"] and "model" not in b["config"]
+
+
+def test_clock_summary_reads_nvidia_smi_samples():
+    """The `clocks` object of the GPU line: median SM clock under load, the maximum, and
+    every throttle reason seen Active in any sample (the ones that reject a run among
+    them); malformed or partial lines are skipped."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    clk = bench.ClockSampler(0)
+    clk.lines = [
+        "0, 2070, 2070, 900.1, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 1950, 2070, 1390.5, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 1000.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, [N/A], 2070, 10.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 2070, 2070",
+    ]
+    s = clk.summary()
+    assert s == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    clk.lines = ["0, 1200, 2070, 700, 0x8, Not Active, Active, Not Active, Not Active"]
+    assert clk.summary()["reasons"] == ["hw_thermal_slowdown"]
+    clk.lines = []
+    assert clk.summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
