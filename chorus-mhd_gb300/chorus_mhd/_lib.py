@@ -28,7 +28,8 @@ class ChorusParams(ctypes.Structure):
 
 
 class ChorusServeRequest(ctypes.Structure):
-    _fields_ = [("case_dir", c_char_p), ("arrival_s", c_double), ("end_time", c_double)]
+    _fields_ = [("case_dir", c_char_p), ("arrival_s", c_double), ("end_time", c_double),
+                ("Q_out", ctypes.POINTER(c_double)), ("Q_out_count", ctypes.c_int64), ("restart_path", c_char_p)]
 
 
 class ChorusServeConfig(ctypes.Structure):
@@ -37,8 +38,8 @@ class ChorusServeConfig(ctypes.Structure):
 
 
 class ChorusServeResult(ctypes.Structure):
-    _fields_ = [("admit_s", c_double), ("finish_s", c_double), ("latency_s", c_double), ("dof", ctypes.c_int64),
-                ("steps", c_int), ("status", c_int)]
+    _fields_ = [("admit_s", c_double), ("finish_s", c_double), ("latency_s", c_double), ("wait_s", c_double),
+                ("ctime", c_double), ("dof", ctypes.c_int64), ("steps", c_int), ("status", c_int)]
 
 
 class ChorusDiag(ctypes.Structure):
@@ -83,6 +84,7 @@ SIGNATURES = {
     "chorus_gpu_profile_stage": (c_int, [c_void_p, c_int, dp]),
     "chorus_gpu_launch_counts": (c_int, [c_void_p, ip, ip]),
     "chorus_gpu_device_bytes": (ctypes.c_int64, [c_void_p]),
+    "chorus_gpu_fp64_fma_peak": (c_int, [c_int, dp, dp]),
     "chorus_batch_create": (c_int, [c_int, P(c_void_p)]),
     "chorus_batch_free": (c_int, [c_void_p]),
     "chorus_batch_add": (c_int, [c_void_p, c_void_p, ip]),

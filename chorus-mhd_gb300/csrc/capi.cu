@@ -1403,7 +1403,11 @@ int chorus_write_restart(ChorusCtx* c, const char* path, int32_t iter, double ct
 int chorus_read_restart(ChorusCtx* c, const char* path, int32_t* iter, double* ctime) {
   if (!c || !path) return set_err(CHORUS_EINVAL, "null argument");
   const int N = c->dims.N, NC = c->dims.NCELL, nq = 9 * N * N;
+  // a cell the stream does not name keeps its current state, as in READ_ALL_DATA_BINARY
+  // (read_data_restart.f90:55-56 assigns only the cells it reads)
   std::vector<double> Q((size_t)NC * nq, 0.0);
+  int rc0 = chorus_gpu_download_state(c, Q.data());
+  if (rc0) return rc0;
   FILE* f = std::fopen(path, "rb");
   if (!f) return set_err(CHORUS_EIO, "cannot open %s", path);
   int32_t it = 0;

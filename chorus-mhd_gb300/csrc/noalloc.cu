@@ -11,12 +11,20 @@
 // staging area in a fixed array compiled into this file, so it allocates nothing.
 //
 // The array holds kNoAllocMaxPoints points (10 MiB of device memory on every GPU that
-// loads the library, kept until the process exits).  Its device address is looked up
-// once per device, with that device current, on the first call made on that device;
-// make that first call before any stream capture.  All calls share the one array and it
-// keeps the last call's contents: every output slot is rewritten for the points of the
-// current call, so nothing needs clearing, but calls that overlap on the GPU (from two
-// host threads, or while a previous call is still running) race on the array.
+// loads the library, kept until the process exits).  With CUDA's lazy module loading
+// (the default) the array is reserved when this file's module is first used on a
+// device, which is the set-up of the first call on that device: that call needs 10 MiB
+// of free device memory, so a host that hands all its memory to a pool makes one call
+// with n = 0 (set-up only) before it builds the pool.  The set-up, once per device with
+// that device current, looks up the array's device address and creates the stream the
+// copies and the kernel run on (non-blocking, so a call does not wait for, or hold up,
+// the host's own work on other streams); make the first call before any stream capture.
+// A CUDA error drops the device's set-up so the next call redoes it; calls made after
+// cudaDeviceReset of a device without such an error are not supported.
+// All calls share the one array and it keeps the last call's contents: every output
+// slot is rewritten for the points of the current call, so nothing needs clearing, but
+// calls that overlap on the GPU (from two host threads, or while a previous call is
+// still running) race on the array.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -38,8 +46,9 @@ __device__ __align__(256) double g_rusanov_scratch[kNoAllocMaxPoints * kNoAllocP
 
 std::mutex g_scratch_mu;
 double* g_scratch_addr[64] = {nullptr};
+cudaStream_t g_scratch_stream[64] = {nullptr};
 
-int scratch_for_current_device(double** out) {
+int scratch_for_current_device(double** out, cudaStream_t* st, int* dev_out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return chorus::set_err(CHORUS_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
@@ -50,10 +59,27 @@ int scratch_for_current_device(double** out) {
     e = cudaGetSymbolAddress(&p, g_rusanov_scratch);
     if (e != cudaSuccess || !p)
       return chorus::set_err(CHORUS_ECUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", dev, cudaGetErrorString(e));
+    if (!g_scratch_stream[dev]) {
+      e = cudaStreamCreateWithFlags(&g_scratch_stream[dev], cudaStreamNonBlocking);
+      if (e != cudaSuccess) {
+        g_scratch_stream[dev] = nullptr;
+        return chorus::set_err(CHORUS_ECUDA, "cudaStreamCreateWithFlags on device %d: %s", dev, cudaGetErrorString(e));
+      }
+    }
     g_scratch_addr[dev] = static_cast<double*>(p);
   }
   *out = g_scratch_addr[dev];
+  *st = g_scratch_stream[dev];
+  *dev_out = dev;
   return CHORUS_OK;
+}
+
+// after a CUDA error the next call on the device looks the address up again (the stream
+// handle is dropped without destroying it: it may belong to a context that is gone)
+void drop_setup(int dev) {
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  g_scratch_addr[dev] = nullptr;
+  g_scratch_stream[dev] = nullptr;
 }
 
 }  // namespace
@@ -65,12 +91,14 @@ extern "C" int getrusanovflux_noalloc_gpu(int32_t n, double gam, const double* Q
   if (n > kNoAllocMaxPoints)
     return chorus::set_err(CHORUS_EINVAL, "getrusanovflux_noalloc_gpu: n=%d exceeds the fixed capacity of %d points", n,
                            kNoAllocMaxPoints);
-  if (n == 0) return CHORUS_OK;
+  double* base = nullptr;
+  cudaStream_t st = nullptr;
+  int dev = 0;
+  int rc = scratch_for_current_device(&base, &st, &dev);
+  if (rc) return rc;
+  if (n == 0) return CHORUS_OK;  // set-up only
   if (!Qfl || !Qfr || !Fnl || !Fnr || !Az || !normf || !sign_l || !sign_r || !eigv)
     return chorus::set_err(CHORUS_EINVAL, "getrusanovflux_noalloc_gpu: null argument");
-  double* base = nullptr;
-  int rc = scratch_for_current_device(&base);
-  if (rc) return rc;
   const size_t m = (size_t)n;
   double* dQl = base;
   double* dQr = base + 9 * m;
@@ -81,18 +109,25 @@ extern "C" int getrusanovflux_noalloc_gpu(int32_t n, double gam, const double* Q
   double* dev_ = base + 37 * m;
   int* dsl = reinterpret_cast<int*>(base + 38 * m);
   int* dsr = dsl + m;
-  cudaError_t e = cudaMemcpy(dQl, Qfl, 9 * m * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(dQr, Qfr, 9 * m * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(dnf, normf, 2 * m * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(dsl, sign_l, m * sizeof(int), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(dsr, sign_r, m * sizeof(int), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return chorus::set_err(CHORUS_ECUDA, "getrusanovflux_noalloc_gpu upload: %s", cudaGetErrorString(e));
-  chorus::launch_point_rusanov(n, gam, dQl, dQr, dFl, dFr, dAz, dnf, dsl, dsr, dev_, 0);
+  cudaError_t e = cudaMemcpyAsync(dQl, Qfl, 9 * m * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dQr, Qfr, 9 * m * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dnf, normf, 2 * m * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dsl, sign_l, m * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dsr, sign_r, m * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) {
+    drop_setup(dev);
+    return chorus::set_err(CHORUS_ECUDA, "getrusanovflux_noalloc_gpu upload: %s", cudaGetErrorString(e));
+  }
+  chorus::launch_point_rusanov(n, gam, dQl, dQr, dFl, dFr, dAz, dnf, dsl, dsr, dev_, st);
   e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpy(Fnl, dFl, 8 * m * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(Fnr, dFr, 8 * m * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(Az, dAz, m * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(eigv, dev_, m * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return chorus::set_err(CHORUS_ECUDA, "getrusanovflux_noalloc_gpu: %s", cudaGetErrorString(e));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Fnl, dFl, 8 * m * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Fnr, dFr, 8 * m * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Az, dAz, m * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(eigv, dev_, m * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    drop_setup(dev);
+    return chorus::set_err(CHORUS_ECUDA, "getrusanovflux_noalloc_gpu: %s", cudaGetErrorString(e));
+  }
   return CHORUS_OK;
 }

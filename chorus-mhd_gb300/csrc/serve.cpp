@@ -9,6 +9,10 @@
 // returns to the budget, after its last step.  Mode 1 is the plain sequential loop the
 // batched form is compared with: requests run one at a time, first come first served,
 // each with its own single-solve CUDA graph.
+//
+// A retiring solve hands back its result before its memory is released: the final Q in
+// the reference layout into the request's Q_out and/or the restart stream of
+// write_data.f90:44-74 at restart_path.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -45,7 +49,8 @@ void wait_until(std::chrono::steady_clock::time_point t0, double t) {
   if (d > 0) std::this_thread::sleep_for(std::chrono::duration<double>(d));
 }
 
-int open_request(const ChorusServeRequest& r, int device, Live& L, int64_t* dof, int32_t* steps) {
+int open_request(const ChorusServeRequest& r, int device, Live& L, int64_t* dof, int32_t* steps, double* ctime) {
+  (void)device;
   int rc = chorus_mesh_load(r.case_dir, &L.mesh);
   if (rc) return rc;
   ChorusDims d;
@@ -56,7 +61,22 @@ int open_request(const ChorusServeRequest& r, int device, Live& L, int64_t* dof,
   if (L.steps_left < 1) L.steps_left = 1;
   *dof = (int64_t)d.NCELL * d.N * d.N;
   *steps = (int32_t)L.steps_left;
+  // ctime of the reference's bookkeeping: dt added once per step (iterations.f90:162-217)
+  double t = 0.0;
+  for (int64_t k = 0; k < L.steps_left; k++) t = t + p.dt;
+  *ctime = t;
+  if (r.Q_out && r.Q_out_count != (int64_t)9 * d.N * d.N * d.NCELL)
+    return chorus::set_err(CHORUS_EINVAL, "request %s: Q_out_count %lld, the state has %lld doubles", r.case_dir,
+                           (long long)r.Q_out_count, (long long)9 * d.N * d.N * d.NCELL);
   return CHORUS_OK;
+}
+
+// hand back a finished solve's state (before its context is freed)
+int deliver(const ChorusServeRequest& r, const ChorusServeResult& res, ChorusCtx* ctx) {
+  int rc = CHORUS_OK;
+  if (r.Q_out) rc = chorus_gpu_download_state(ctx, r.Q_out);
+  if (!rc && r.restart_path) rc = chorus_write_restart(ctx, r.restart_path, res.steps, res.ctime);
+  return rc;
 }
 
 void close_live(Live& L) {
@@ -86,18 +106,21 @@ extern "C" int chorus_serve_run(const ChorusServeRequest* reqs, int32_t n, const
       Live L;
       int64_t dof = 0;
       int32_t steps = 0;
+      double ctime_end = 0.0;
       out[i].admit_s = now_s(t0);
-      int rc = open_request(reqs[i], dev, L, &dof, &steps);
+      int rc = open_request(reqs[i], dev, L, &dof, &steps, &ctime_end);
       if (!rc) rc = chorus_gpu_bind_mesh(L.mesh, dev, &L.ctx);
       if (!rc) rc = chorus_initial_state(L.mesh, L.ctx, nullptr);
       if (!rc) rc = chorus_gpu_set_option(L.ctx, "diagnostics", 0);
       int32_t it = 0;
       double ct = 0.0;
       if (!rc) rc = iterations_gpu(L.ctx, steps, &it, &ct, nullptr, 0, nullptr);
-      out[i].finish_s = now_s(t0);
-      out[i].latency_s = out[i].finish_s - reqs[i].arrival_s;
       out[i].steps = steps;
       out[i].dof = dof;
+      out[i].ctime = ctime_end;
+      if (!rc) rc = deliver(reqs[i], out[i], L.ctx);
+      out[i].finish_s = now_s(t0);
+      out[i].latency_s = out[i].finish_s - reqs[i].arrival_s;
       out[i].status = rc;
       close_live(L);
     }
@@ -115,7 +138,9 @@ extern "C" int chorus_serve_run(const ChorusServeRequest* reqs, int32_t n, const
   bool running = false;  // a batch step is in flight
   Live pending;          // read (mesh maps built) but waiting for device memory
   bool have_pending = false;
+  double blocked_since = -1.0;  // when the pending request was first refused for memory
   auto finish = [&](Live& L, int status) {
+    if (status == CHORUS_OK && L.ctx) status = deliver(reqs[L.req], out[L.req], L.ctx);
     out[L.req].finish_s = now_s(t0);
     out[L.req].latency_s = out[L.req].finish_s - reqs[L.req].arrival_s;
     out[L.req].status = status;
@@ -129,21 +154,28 @@ extern "C" int chorus_serve_run(const ChorusServeRequest* reqs, int32_t n, const
         if (reqs[next].arrival_s > now_s(t0)) break;
         int64_t dof = 0;
         int32_t steps = 0;
+        double ctime_end = 0.0;
         pending = Live();
         pending.req = next;
-        rc = open_request(reqs[next], dev, pending, &dof, &steps);
+        rc = open_request(reqs[next], dev, pending, &dof, &steps, &ctime_end);
         out[next].dof = dof;
         out[next].steps = steps;
+        out[next].ctime = ctime_end;
         next++;
         if (rc) { finish(pending, rc); continue; }
         if (pending.bytes > budget) { finish(pending, CHORUS_ENOMEM); continue; }
         have_pending = true;
       }
-      if (used + pending.bytes > budget) break;  // wait until memory returns
-      if (cfg->max_active > 0 && (int)(live.size() + ready.size()) >= cfg->max_active) break;
+      if (used + pending.bytes > budget ||
+          (cfg->max_active > 0 && (int)(live.size() + ready.size()) >= cfg->max_active)) {
+        if (blocked_since < 0) blocked_since = now_s(t0);  // wait until memory returns
+        break;
+      }
       Live L = pending;
       have_pending = false;
       out[L.req].admit_s = now_s(t0);
+      out[L.req].wait_s = blocked_since < 0 ? 0.0 : out[L.req].admit_s - blocked_since;
+      blocked_since = -1.0;
       rc = chorus_gpu_bind_mesh(L.mesh, dev, &L.ctx);
       if (!rc) rc = chorus_initial_state(L.mesh, L.ctx, nullptr);
       if (rc) { finish(L, rc); continue; }

@@ -117,7 +117,10 @@ int chorus_gpu_get_eigvmax(ChorusCtx* ctx, double* eigvmax_g, double* epsilon0);
 /* compresid.f90:1-67 (calls compflux.f90:1-31 and everything below it); the result
  * stays on the device in "resid". */
 int compresid_gpu(ChorusCtx* ctx);
-/* compflux.f90:33-49 comp_inviscid_flux (F1/G2, Qvfi/Qvfj, Azfi/Azfj, eigvmax). */
+/* compflux.f90:33-49 comp_inviscid_flux (F1/G2, Qvfi/Qvfj, Azfi/Azfj, eigvmax).  The
+ * reference's routine raises the module's eigvmax, which compflux zeroes before calling
+ * it; here every evaluation starts it from zero, so chorus_gpu_get_eigvmax afterwards
+ * gives the maximum wave speed over this evaluation's faces. */
 int comp_inviscid_flux_gpu(ChorusCtx* ctx);
 /* compflux.f90:107-157 nablaQsp(v_sta,v_end) on the current Qvfi/Qvfj (1-based
  * variable range, by reference like the Fortran call). */
@@ -190,8 +193,14 @@ int getvfluxvectors_av_c(ChorusCtx* ctx, const double* Qv, const double* nablaQ,
  * work in flight that a cudaFree would stall.  Same arguments and results; the device
  * staging lives in a fixed 10 MiB array inside the library, so n is limited to 32768
  * points per call (larger n returns CHORUS_EINVAL) and no cudaMalloc/cudaFree is made.
- * The first call on a device looks up the array's address (make it before any stream
- * capture).  All calls share the array: calls that overlap on the GPU race. */
+ * The first call on a device does its set-up: it looks up the array's address and
+ * creates the non-blocking stream the copies and the kernel run on, and under CUDA's
+ * lazy module loading that is also when the 10 MiB are reserved -- so it needs that much
+ * free device memory.  A call with n = 0 does the set-up alone: a host that hands all
+ * its device memory to a pool makes it first; make it before any stream capture.  A
+ * CUDA error drops the set-up (the next call redoes it); calls after cudaDeviceReset
+ * without such an error are not supported.  All calls share the array: calls that
+ * overlap on the GPU race. */
 int getrusanovflux_noalloc_gpu(int32_t n, double gam, const double* Qfl, const double* Qfr, double* Fnl,
                                double* Fnr, double* Az, const double* normf, const int32_t* sign_l,
                                const int32_t* sign_r, double* eigv);
@@ -228,6 +237,11 @@ int64_t chorus_gpu_get_option(ChorusCtx* ctx, const char* name);
 int chorus_gpu_launch_counts(ChorusCtx* ctx, int32_t* per_step, int32_t* per_diag);
 /* Device bytes held by ctx (state, work arrays, geometry). */
 int64_t chorus_gpu_device_bytes(ChorusCtx* ctx);
+/* The FP64 pipe's measured fused multiply-add rate on `device` (FMA per second; each FMA
+ * is two flops): independent fma chains over 64 warps per SM, timed with CUDA events
+ * after a warm-up launch.  *ms = the timed launches' duration (may be NULL).  The
+ * residual path's FP64 instruction rate is reported against it. */
+int chorus_gpu_fp64_fma_peak(int32_t device, double* fma_per_s, double* ms);
 
 /* ------------------------------------------------------------------------------
  * Batched form: many independent solves (any N, size, problem, dt) advanced together,
@@ -262,6 +276,16 @@ typedef struct ChorusServeRequest {
   const char* case_dir; /* QUAD.INP + mesh files */
   double arrival_s;     /* seconds after the start of the run (sorted ascending) */
   double end_time;      /* physical end time of the solve */
+  /* Results of the solve (each may be NULL):
+   *   Q_out        receives the final state Q(9,N,N,NCELL) in the reference layout when the
+   *                solve retires; Q_out_count must then equal 9*N*N*NCELL (else the request
+   *                fails with CHORUS_EINVAL before any device work);
+   *   restart_path receives the final state as the restart stream of write_data.f90:44-74
+   *                (iter = steps run, ctime = their sum of dt), readable by
+   *                chorus_read_restart and by the reference's READ_ALL_DATA_BINARY. */
+  double* Q_out;
+  int64_t Q_out_count;
+  const char* restart_path;
 } ChorusServeRequest;
 typedef struct ChorusServeConfig {
   int32_t device;
@@ -272,6 +296,8 @@ typedef struct ChorusServeConfig {
 } ChorusServeConfig;
 typedef struct ChorusServeResult {
   double admit_s, finish_s, latency_s; /* seconds since start; latency = finish - arrival */
+  double wait_s;  /* time an arrived request waited for device memory (admission control) */
+  double ctime;   /* physical time reached: steps x dt, accumulated as the reference does */
   int64_t dof;
   int32_t steps;
   int32_t status; /* CHORUS_OK or the error of that request */

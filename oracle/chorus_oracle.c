@@ -2000,6 +2000,7 @@ int orc_setd(orc_t* o, const char* n, double v) {
   else if (!strcmp(n, "ctime")) o->ctime = v;
   else if (!strcmp(n, "mu")) o->mu = v;
   else if (!strcmp(n, "eta0")) o->eta0 = v;
+  else if (!strcmp(n, "eigvmax")) o->eigvmax = v;
   else return -1;
   return 0;
 }

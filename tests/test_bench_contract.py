@@ -25,6 +25,10 @@ def test_reference_arm_prints_the_contract_line():
     assert b["cpu_baseline"]["kind"] in ("port", "reference")
     assert b["e2e"]["value"] == b["value"] and b["e2e"]["h2d_bytes_per_step"] == 0
     assert "workload" in b["config"] and "model" not in b["config"]
+    # the same config dict as the GPU arm's (bench.config_dict), window included
+    assert b["config"]["window"] == "steps 1000-1000 of the 1000-step run"
+    for k in ("cells", "N", "dof", "stages_per_step", "l2", "parallelism"):
+        assert k in b["config"], k
 
 
 def test_clock_summary_reads_nvidia_smi_samples():

@@ -80,6 +80,28 @@ def test_one_stage_arrays_match_oracle(case_root, case):
     assert abs(ev - o.getd("eigvmax")) <= 1e-13 * o.getd("eigvmax")
 
 
+@pytest.mark.parametrize("case", CASES[:4] + CASES[6:9], ids=ids)
+def test_comp_inviscid_flux_drop_in_matches_oracle(case_root, case):
+    """comp_inviscid_flux_gpu alone (compflux.f90:33-49): the interior and face
+    inviscid fluxes F1/G2, the face-averaged traces Qvfi/Qvfj, the upwinded A_z traces
+    Azfi/Azfj and the stage's maximum wave speed, on the oracle's state after two steps."""
+    d = make_case(case_root, **case)
+    o = oracle.Oracle(d)
+    o.run(2)
+    s = Solver(Mesh(d), initial_state=False)
+    s.upload(o.array("Q").copy())
+    # the reference's routine only raises the module's eigvmax, which compflux zeroes
+    # before it (compflux.f90:1-31); the drop-in reports the maximum of its own faces
+    o.setd("eigvmax", 0.0)
+    o.comp_inviscid_flux()
+    s.comp_inviscid_flux()
+    sz = reference_layout_sizes(s.N, s.ncell)
+    for name in ["F1", "G2", "Qvfi", "Qvfj", "Azfi", "Azfj"]:
+        assert_close(s.array(name, sz[name]), o.array(name), STAGE_TOL, name)
+    ev, _ = s.eigvmax()
+    assert abs(ev - o.getd("eigvmax")) <= 1e-13 * o.getd("eigvmax")
+
+
 @pytest.mark.parametrize("case", CASES, ids=ids)
 def test_run_matches_oracle(case_root, case):
     """iterations: RK steps + CT projection + diagnostics vs the oracle."""

@@ -10,6 +10,7 @@ import ctypes
 import numpy as np
 import pytest
 
+import oracle
 from chorus_mhd import _lib
 
 TOL = 1e-12  # the point-function tolerance used by tests/test_gpu_points.py
@@ -60,6 +61,46 @@ def test_no_alloc_rusanov_matches_allocating_entry_point_twice():
             scale = np.abs(b).max() + 1.0
             assert np.all(np.isfinite(a)), name
             assert np.abs(a - b).max() <= TOL * scale, "call %d: %s differs" % (call + 1, name)
+
+
+def _inputs(seed, n, gam):
+    rng = np.random.default_rng(seed)
+    Ql, Qr = _states(rng, n, gam), _states(rng, n, gam)
+    nf = rng.uniform(-2, 2, (n, 2))
+    sl = rng.choice([-1, 1], n).astype(np.int32)
+    sr = rng.choice([-1, 1], n).astype(np.int32)
+    return Ql, Qr, nf, sl, sr
+
+
+@pytest.mark.gpu
+def test_no_alloc_full_capacity_matches_oracle_and_allocates_nothing():
+    """n equal to the capacity (the last slot of every region of the array is written)
+    against the oracle's getrusanovflux point by point and against getrusanovflux_gpu; a
+    second call leaves the device's free memory unchanged."""
+    import torch
+    L = _lib.load()
+    gam = 1.4
+    assert L.getrusanovflux_noalloc_gpu(0, gam, None, None, None, None, None, None, None, None, None) == 0  # set-up
+    n = MAX_POINTS
+    args = _inputs(7, n, gam)
+    got = _call(L.getrusanovflux_noalloc_gpu, n, gam, *args)
+    ref = _call(L.getrusanovflux_gpu, n, gam, *args)
+    Ql, Qr, nf, sl, sr = args
+    orc = [np.zeros((n, 8)), np.zeros((n, 8)), np.zeros(n), np.zeros(n)]
+    for i in range(n):
+        Fl, Fr, az, ev = oracle.getrusanovflux(gam, Ql[i], Qr[i], nf[i], sl[i], sr[i])
+        orc[0][i], orc[1][i], orc[2][i], orc[3][i] = Fl, Fr, az, ev
+    for a, b, c, name in zip(got, ref, orc, ["Fnl", "Fnr", "Az", "eigv"]):
+        scale = np.abs(c).max() + 1.0
+        assert np.all(np.isfinite(a)), name
+        assert np.abs(a - c).max() <= TOL * scale, "%s differs from the oracle" % name
+        assert np.abs(a - b).max() <= TOL * scale, "%s differs from getrusanovflux_gpu" % name
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    again = _call(L.getrusanovflux_noalloc_gpu, n, gam, *_inputs(8, n, gam))
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0, "a call changed the device's free memory by %d bytes" % (free0 - free1)
+    assert all(np.all(np.isfinite(a)) for a in again)
 
 
 @pytest.mark.gpu
