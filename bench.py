@@ -653,6 +653,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-other-workloads", action="store_true")
+    ap.add_argument("--run-steps", type=int, default=None,
+                    help="length of the run whose last --steps steps are timed (default: the configuration's "
+                         "stated run; a short run keeps profiler captures small)")
     ap.add_argument("--prepare-window-state", nargs=3, metavar=("CASE", "STEP", "OUT"), default=None,
                     help=argparse.SUPPRESS)
     ap.add_argument("--ensemble-count", type=int, default=256)
@@ -667,6 +670,8 @@ def main():
     args = ap.parse_args()
     MU, ETA0 = args.mu, args.eta0
     WORKLOAD = args.workload
+    if args.run_steps:
+        RUN_STEPS[WORKLOAD] = max(args.run_steps, 1)
     w = WORKLOADS[args.workload]
     PROBLEM, JITTER, SEED = w["problem"], w["jitter"], w["seed"]
     NX = args.nx if args.nx else w["nx"]

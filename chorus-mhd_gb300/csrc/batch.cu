@@ -1,14 +1,16 @@
 // batch.cu -- many independent solves of mixed size and order advanced together:
 // one launch per pass for the whole ensemble.
 //
-// Each pass is a persistent kernel (a fixed grid of CTAs sized to the GPU) that pulls
-// tiles from a device work table with an atomic counter.  A cell tile is
-// (solve, first cell, cells, N), a face tile (solve, first face point, points, N); the
-// kernel copies the tile's solve descriptor to shared memory and runs the same
-// per-N pass body as the single-solve kernels, so a solve gives the same bits alone and
-// in a batch.  Tables, counts and per-solve RK coefficients live in device memory and
-// are rewritten between steps, so one captured CUDA graph serves any composition that
-// fits the table capacities (the serving loop changes the mix every step).
+// Each pass is one launch per order N present in the batch: a persistent kernel (a grid
+// of CTAs sized by occupancy to fill the GPU) specialised for N, with the launch shape
+// tuned for N, walking that order's tiles with a static stride.  A cell tile is
+// (solve, first cell, cells), a face tile (solve, first face point, points); the kernel
+// copies the tile's solve descriptor to shared memory and runs the same per-N pass body
+// as the single-solve kernels, so a solve gives the same bits alone and in a batch.
+// Tables, counts and per-solve RK coefficients live in device memory and are rewritten
+// between steps, so one captured CUDA graph serves any composition whose orders it
+// already launches and that fits the table capacities (the serving loop changes the mix
+// every step).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,13 +38,18 @@ void upload_ops_all(int N, const OpsN& o) {
   cudaMemcpyToSymbol(c_ops_all, &o, sizeof(OpsN), sizeof(OpsN) * N);
 }
 
+// passes of a step, in the order of the tile tables
+enum { PE1 = 0, PF1, PE2, PE3, PCT, PCTF, kPasses };
+constexpr int kGroups = kPasses * (kMaxN + 1);
+__host__ __device__ constexpr int gidx(int pass, int N) { return pass * (kMaxN + 1) + N; }
+
 struct BatchDev {
-  const SolveDev* solves;   // per slot (eig/err point into the batch's own arrays)
-  const int4* ctiles;       // (slot, e0, cnt, N): the E1, E2, E3 and CT tile lists, one after another
-  const int4* ftiles;       // (slot, t0, cnt, N)
-  const int* ntiles;        // [0] E1 tiles, [1] face tiles, [2] E2 tiles, [3] E3 tiles, [4] CT tiles
-  int* counters;            // per-launch tile counters, zeroed at the start of each stage
-  const RKStage* rk;        // [5][cap]
+  const SolveDev* solves;  // per slot (eig/err point into the batch's own arrays)
+  const int4* ctiles;      // cell tiles (slot, first cell, cells, 0) of every cell pass and order
+  const int4* ftiles;      // face tiles (slot, first face point, points, 0)
+  const int* gcount;       // [pass][N] tiles of that pass and order
+  const int* goff;         // [pass][N] their first entry in ctiles / ftiles
+  const RKStage* rk;       // [5][cap]
   int cap;
   int pad;
 };
@@ -60,31 +67,147 @@ __device__ __forceinline__ const SolveDev& load_solve(const SolveDev* src) {
   return ss;
 }
 
-// Walks a tile list with a persistent CTA: thread 0 claims the next tile with an atomic
-// issued before the current tile's work (its latency overlaps the work), and the solve
-// descriptor is copied to shared memory only when the solve changes.  body(T, s) runs
-// with the whole CTA.
+// A CTA of a pass kernel for order N walks the pass's tiles of that order with a static
+// stride (tile blockIdx.x, then + gridDim.x, ...): consecutive tiles of one solve go to
+// consecutive CTAs, and the solve descriptor is copied to shared memory only when the
+// solve changes.  body(T, s) runs with the whole CTA; a barrier separates tiles.
 template <class Body>
-__device__ __forceinline__ void for_each_tile(int* counter, int nt, const int4* tiles, const SolveDev* solves,
-                                              Body&& body) {
-  __shared__ int cur;
-  if (threadIdx.x == 0) cur = atomicAdd(counter, 1);
-  __syncthreads();
-  int ti = cur, slot = -1;
+__device__ __forceinline__ void for_tiles(const BatchDev& b, int g, const int4* tiles, Body&& body) {
+  const int cnt = b.gcount[g];
+  const int4* t = tiles + b.goff[g];
+  int slot = -1;
   const SolveDev* s = nullptr;
-  while (ti < nt) {
-    int nxt = 0;
-    if (threadIdx.x == 0) nxt = atomicAdd(counter, 1);  // consumed after the tile
-    const int4 T = tiles[ti];
+  for (int ti = blockIdx.x; ti < cnt; ti += gridDim.x) {
+    const int4 T = t[ti];
     if (T.x != slot) {
-      s = &load_solve(solves + T.x);  // ends with a barrier
+      s = &load_solve(b.solves + T.x);  // ends with a barrier
       slot = T.x;
     }
     body(T, *s);
-    __syncthreads();  // every thread is done with this tile
-    if (threadIdx.x == 0) cur = nxt;
+    __syncthreads();  // every thread is done with this tile's shared memory
+  }
+}
+
+// One kernel per pass and order N, launched only for the orders present in the batch,
+// each with the launch shape tuned for its order and the register budget of its own
+// body, running the same per-N bodies as the single-solve kernels (so a solve gives the
+// same bits alone and in a batch).
+template <int N>
+__global__ void __launch_bounds__(512, 2) kg_e1(BatchDev b, int sensor_on) {
+  extern __shared__ __align__(16) double sm[];
+  pdl_wait();
+  for_tiles(b, gidx(PE1, N), b.ctiles, [&](const int4& T, const SolveDev& s) {
+    if (T.y == 0 && threadIdx.x == 0) *s.eig = 0ull;  // the solve's stage starts its wave-speed maximum
+    // 1: variable-1 sensor; 3: also variable 6 when the solve's plot flag is set
+    const int sensor = s.artiv ? ((sensor_on & 2) && !*s.plot_flag ? 1 : sensor_on) : 0;
+    e1_body<N, OpsAll<N>>(s, T.y, T.z, T.z, sensor, sm);
+  });
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) kg_f1(BatchDev b) {
+  pdl_wait();
+  for_tiles(b, gidx(PF1, N), b.ftiles, [&](const int4& T, const SolveDev& s) {
+    unsigned long long evb = 0ull;
+    if ((int)threadIdx.x < T.z) evb = f1_point<N>(s, T.y + threadIdx.x);
+    block_max_ull(evb, s.eig);
+  });
+}
+
+// E2 tiles are chunks of up to blockDim.x cells, compacted to the cells that need
+// gradients and run in groups of epb (as k_e2)
+template <int N>
+__global__ void __launch_bounds__(512) kg_e2(BatchDev b, int epb) {
+  extern __shared__ __align__(16) double sm[];
+  pdl_wait();
+  for_tiles(b, gidx(PE2, N), b.ctiles, [&](const int4& T, const SolveDev& s) {
+    e2_chunk<N, OpsAll<N>>(s, T.y, T.z, epb, sm);
+  });
+}
+
+template <int N>
+__global__ void __launch_bounds__(512, 2) kg_e3(BatchDev b, int stage) {
+  extern __shared__ __align__(16) double sm[];
+  __shared__ __align__(16) RKStage srk;
+  pdl_wait();
+  for_tiles(b, gidx(PE3, N), b.ctiles, [&](const int4& T, const SolveDev& s) {
+    if (threadIdx.x == 0) srk = b.rk[stage * b.cap + T.x];
     __syncthreads();
-    ti = cur;
+    e3_body<N, OpsAll<N>>(s, T.y, T.z, T.z, srk, 1, sm);
+  });
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) kg_ct(BatchDev b, int mode) {
+  extern __shared__ __align__(16) double sm[];
+  pdl_wait();
+  for_tiles(b, gidx(PCT, N), b.ctiles, [&](const int4& T, const SolveDev& s) {
+    ct_elem_body<N, OpsAll<N>>(s, T.y, T.z, T.z, mode, sm);
+  });
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) kg_ctface(BatchDev b) {
+  pdl_wait();
+  for_tiles(b, gidx(PCTF, N), b.ftiles, [&](const int4& T, const SolveDev& s) {
+    if ((int)threadIdx.x < T.z) ctface_point<N>(s, T.y + threadIdx.x);
+  });
+}
+
+// dynamic shared memory of a cell pass (0 E1, 1 E2, 2 E3, 3 CT) on tiles of epb cells
+size_t cell_smem_bytes(int N, int epb, int pass) {
+  const int NS = N * N, NFP = 2 * (N + 1) * N;
+  size_t d = 0;
+  switch (pass) {
+    case 0: d = (size_t)epb * (NS * 9 + 2 * NS + NFP * 9) + N * N; break;
+    case 1: d = (size_t)epb * (NFP * 16 + NS * 17); break;
+    case 2: d = (size_t)epb * (NFP * 8 + NS * (1 + 9 + 1 + 2) + NFP * 2); break;
+    default: d = (size_t)epb * (NFP * 2 + NS * 2); break;
+  }
+  return sizeof(double) * d;
+}
+
+}  // namespace
+
+// launch shape of one pass kernel of one order
+struct PassShape {
+  int threads = 0, grid = 0, epb = 0;
+  size_t smem = 0;
+};
+
+// the launches of order N: shapes filled on first use (occupancy-sized persistent grids)
+template <int N>
+static void pass_shapes(int nsm, const int (&epb)[4], const int (&threads)[4], PassShape (&sh)[kPasses]) {
+  const int lim = 200 * 1024;
+  cudaFuncSetAttribute(kg_e1<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(kg_e2<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(kg_e3<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  cudaFuncSetAttribute(kg_ct<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  auto fill = [&](PassShape& p, const void* fn, int thr, int e, size_t smem) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, thr, smem) != cudaSuccess || occ < 1) occ = 1;
+    p.threads = thr;
+    p.epb = e;
+    p.smem = smem;
+    p.grid = nsm * occ;
+  };
+  fill(sh[PE1], (const void*)kg_e1<N>, threads[0], epb[0], cell_smem_bytes(N, epb[0], 0));
+  fill(sh[PF1], (const void*)kg_f1<N>, 256, 0, 0);
+  fill(sh[PE2], (const void*)kg_e2<N>, threads[1], epb[1], cell_smem_bytes(N, epb[1], 1));
+  fill(sh[PE3], (const void*)kg_e3<N>, threads[2], epb[2], cell_smem_bytes(N, epb[2], 2));
+  fill(sh[PCT], (const void*)kg_ct<N>, threads[3], epb[3], cell_smem_bytes(N, epb[3], 3));
+  fill(sh[PCTF], (const void*)kg_ctface<N>, 256, 0, 0);
+}
+
+template <int N>
+static void launch_pass(const BatchDev& a, int pass, const PassShape& p, cudaStream_t st, int arg) {
+  switch (pass) {
+    case PE1: launch_pdl(kg_e1<N>, p.grid, p.threads, p.smem, st, a, arg); break;
+    case PF1: launch_pdl(kg_f1<N>, p.grid, p.threads, 0, st, a); break;
+    case PE2: launch_pdl(kg_e2<N>, p.grid, p.threads, p.smem, st, a, p.epb); break;
+    case PE3: launch_pdl(kg_e3<N>, p.grid, p.threads, p.smem, st, a, arg); break;
+    case PCT: launch_pdl(kg_ct<N>, p.grid, p.threads, p.smem, st, a, arg); break;
+    default: launch_pdl(kg_ctface<N>, p.grid, p.threads, 0, st, a); break;
   }
 }
 
@@ -100,116 +223,24 @@ __device__ __forceinline__ void for_each_tile(int* counter, int nt, const int4* 
     default: break;                   \
   }
 
-// each cell pass walks its own tile list, cut with that pass's cells per CTA.  The
-// multi-order bodies need more registers than any single order; E1 and E3 are held to
-// 64 (4 and 8 CTAs per SM), which measured faster than fewer CTAs without spills
-__global__ void __launch_bounds__(256, 4) kb_e1(BatchDev b, int slot, int sensor_on) {
-  extern __shared__ __align__(16) double sm[];
-  pdl_wait();
-  for_each_tile(b.counters + slot, b.ntiles[0], b.ctiles, b.solves, [&](const int4& T, const SolveDev& s) {
-    if (T.y == 0 && threadIdx.x == 0) *s.eig = 0ull;  // the solve's stage starts its wave-speed maximum
-    // 1: variable-1 sensor; 3: also variable 6 when the solve's plot flag is set
-    const int sensor = s.artiv ? ((sensor_on & 2) && !*s.plot_flag ? 1 : sensor_on) : 0;
-#define CALL(n) e1_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sensor, sm)
-    CHORUS_BATCH_SWITCH(T.w, CALL)
-#undef CALL
-  });
-}
-
-__global__ void __launch_bounds__(256) kb_e2(BatchDev b, int slot) {
-  extern __shared__ __align__(16) double sm[];
-  pdl_wait();
-  for_each_tile(b.counters + slot, b.ntiles[2], b.ctiles + b.ntiles[0], b.solves,
-                [&](const int4& T, const SolveDev& s) {
-#define CALL(n) e2_body<n, OpsAll<n>>(s, T.y, T.z, T.z, sm)
-                  CHORUS_BATCH_SWITCH(T.w, CALL)
-#undef CALL
-                });
-}
-
-__global__ void __launch_bounds__(128, 8) kb_e3(BatchDev b, int slot, int stage) {
-  extern __shared__ __align__(16) double sm[];
-  pdl_wait();
-  for_each_tile(b.counters + slot, b.ntiles[3], b.ctiles + b.ntiles[0] + b.ntiles[2], b.solves,
-                [&](const int4& T, const SolveDev& s) {
-                  const RKStage& rk = b.rk[stage * b.cap + T.x];
-#define CALL(n) e3_body<n, OpsAll<n>>(s, T.y, T.z, T.z, rk, 1, sm)
-                  CHORUS_BATCH_SWITCH(T.w, CALL)
-#undef CALL
-                });
-}
-
-__global__ void __launch_bounds__(128) kb_ct(BatchDev b, int slot, int mode) {
-  extern __shared__ __align__(16) double sm[];
-  pdl_wait();
-  for_each_tile(b.counters + slot, b.ntiles[4], b.ctiles + b.ntiles[0] + b.ntiles[2] + b.ntiles[3], b.solves,
-                [&](const int4& T, const SolveDev& s) {
-#define CALL(n) ct_elem_body<n, OpsAll<n>>(s, T.y, T.z, T.z, mode, sm)
-                  CHORUS_BATCH_SWITCH(T.w, CALL)
-#undef CALL
-                });
-}
-
-// face passes: which = 0 Rusanov (F1), 1 grad Q trace averages (not part of a step), 2 CT average
-__global__ void __launch_bounds__(128) kb_face(BatchDev b, int slot, int which) {
-  pdl_wait();
-  for_each_tile(b.counters + slot, b.ntiles[1], b.ftiles, b.solves, [&](const int4& T, const SolveDev& s) {
-    // a tile holds 128 to kFaceTileMax points, taken blockDim.x at a time
-    unsigned long long evb = 0ull;
-    for (int base = 0; base < T.z; base += blockDim.x) {
-      const int t = T.y + base + threadIdx.x;
-      if (base + (int)threadIdx.x >= T.z) continue;
-      if (which == 0) {
-        unsigned long long v = 0ull;
-#define CALL(n) v = f1_point<n>(s, t)
-        CHORUS_BATCH_SWITCH(T.w, CALL)
-#undef CALL
-        evb = v > evb ? v : evb;
-      } else if (which == 1) {
-#define CALL(n) f2_point<n>(s, t)
-        CHORUS_BATCH_SWITCH(T.w, CALL)
-#undef CALL
-      } else {
-#define CALL(n) ctface_point<n>(s, t)
-        CHORUS_BATCH_SWITCH(T.w, CALL)
-#undef CALL
-      }
-    }
-    if (which == 0) block_max_ull(evb, s.eig);
-  });
-}
-
-// dynamic shared memory of a cell pass (0 E1, 1 E2, 2 E3, 3 CT) on tiles of epb cells:
-// each pass is launched with its own maximum over the batch, so that one pass's large
-// tiles do not cost the others occupancy
-size_t cell_smem_bytes(int N, int epb, int pass) {
-  const int NS = N * N, NFP = 2 * (N + 1) * N;
-  size_t d = 0;
-  switch (pass) {
-    case 0: d = (size_t)epb * (NS * 9 + 2 * NS + NFP * 9) + N * N; break;
-    case 1: d = (size_t)epb * (NFP * 16 + NS * 17); break;
-    case 2: d = (size_t)epb * (NFP * 8 + NS * (1 + 9 + 1 + 2) + NFP * 2); break;
-    default: d = (size_t)epb * (NFP * 2 + NS * 2); break;
-  }
-  return sizeof(double) * d;
-}
-
-}  // namespace
-
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 struct BatchSlot {
   ChorusCtx* ctx = nullptr;
   SolveDev sd{};
-  int N = 0, NC = 0, nfp_faces = 0;
-  int epb = 4;             // cells per tile of E3 and the CT passes
-  int epb1 = 4, epb2 = 4;  // ... of E1 and E2
-  int epbct = 4;           // ... of the CT element passes
+  int N = 0, NC = 0, nfp_faces = 0, nfp_two = 0;
   double dt = 0.0;
   int k_stage = 3;
   int64_t steps = 0;
   bool active = false;
+};
+
+// launch shapes of one order: cells per tile and threads per CTA of E1, E2, E3, CT
+struct OrderShape {
+  bool used = false;
+  int epb[4] = {0, 0, 0, 0}, threads[4] = {0, 0, 0, 0};
+  PassShape pass[kPasses];
 };
 
 }  // namespace chorus
@@ -230,6 +261,7 @@ void ensure_ops_all(int dev, int N, const ChorusCtx* c);
 
 struct ChorusBatch {
   int device = 0;
+  int nsm = 152;
   cudaStream_t st = nullptr;
   int cap_solves = 0, cap_ctiles = 0, cap_ftiles = 0;
   std::vector<BatchSlot> slots;
@@ -237,24 +269,25 @@ struct ChorusBatch {
   SolveDev* d_solves = nullptr;
   int4* d_ctiles = nullptr;
   int4* d_ftiles = nullptr;
-  int* d_ntiles = nullptr;
-  int* d_counters = nullptr;
+  int* d_gcount = nullptr;  // [kGroups] then d_goff [kGroups]
   RKStage* d_rk = nullptr;
   unsigned long long* d_eig = nullptr;
   unsigned int* d_err = nullptr;
-  int grid_cells = 0, grid_faces = 0;
-  size_t smem[4] = {0, 0, 0, 0};  // per cell pass: E1, E2, E3, CT
+  OrderShape shape[kMaxN + 1];
+  cudaStream_t side[kMaxN + 1] = {};       // one stream per order: the orders' steps are independent chains
+  cudaEvent_t fork = nullptr, join[kMaxN + 1] = {};
+  int cnt[kGroups] = {};                   // tiles per (pass, order) in the tables
   bool dirty = true;
   cudaGraphExec_t graph = nullptr;
-  size_t graph_smem[4] = {0, 0, 0, 0};
+  int graph_grid[kGroups] = {};            // CTAs per launch in the graph (one per tile when captured)
   int ctiles = 0, ftiles = 0;
 };
 
-static constexpr int kCounterSlots = 32;  // one tile counter per launch of a step (5 x 4 + 3)
-static constexpr int kFaceTileMax = 1024;  // face points per tile of the face passes, at most
+static constexpr int kFaceTile = 256;  // face points per tile (one per thread)
 
 static int batch_alloc(ChorusBatch* b, int cap_solves, int cap_ctiles, int cap_ftiles) {
   auto fr = [](void* p) { if (p) cudaFree(p); };
+  cudaStreamSynchronize(b->st);
   fr(b->d_solves); fr(b->d_ctiles); fr(b->d_ftiles); fr(b->d_rk); fr(b->d_eig); fr(b->d_err);
   b->d_solves = nullptr; b->d_ctiles = nullptr; b->d_ftiles = nullptr; b->d_rk = nullptr;
   b->d_eig = nullptr; b->d_err = nullptr;
@@ -273,39 +306,58 @@ static int batch_alloc(ChorusBatch* b, int cap_solves, int cap_ctiles, int cap_f
   return CHORUS_OK;
 }
 
+// the launch shapes of order N, from the first solve of that order (the autotuned shapes
+// of its context); every solve of the order is cut into tiles of those shapes
+static void order_shape(ChorusBatch* b, const BatchSlot& sl) {
+  OrderShape& o = b->shape[sl.N];
+  if (o.used) return;
+  for (int p = 0; p < 4; p++) {
+    o.epb[p] = std::max(1, std::min(ctx_epb(sl.ctx, p), 64));
+    o.threads[p] = std::max(32, std::min(ctx_threads(sl.ctx, p), 512));
+  }
+  // an E2 tile tests up to one cell per thread: a multiple of the group size
+  o.epb[1] = std::min(o.epb[1], o.threads[1]);
+#define CALL(n) pass_shapes<n>(b->nsm, o.epb, o.threads, o.pass)
+  CHORUS_BATCH_SWITCH(sl.N, CALL)
+#undef CALL
+  o.used = true;
+}
+
 static int batch_rebuild(ChorusBatch* b) {
-  std::vector<int> act;
+  // tiles per (pass, order); within an order, larger solves first
+  std::vector<int> order;
   for (int i = 0; i < (int)b->slots.size(); i++)
-    if (b->slots[i].active) act.push_back(i);
-  // tiles: largest N first so the slowest tiles start early
-  std::vector<int4> ct, ft;
-  std::vector<int> order(act);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->slots[a].N > b->slots[c].N; });
-  size_t smem[4] = {0, 0, 0, 0};
-  std::vector<int4> ct2, ct3, ct4;
-  // face tiles: 128 points (one per thread) while the batch is small, up to
-  // kFaceTileMax when there are enough points for about four tiles per CTA
-  long long total_fp = 0;
-  for (int i : order) total_fp += b->slots[i].nfp_faces;
-  int face_tile = (int)std::min<long long>(kFaceTileMax, std::max<long long>(128, total_fp / (4LL * b->grid_faces)));
-  face_tile -= face_tile % 128;
+    if (b->slots[i].active) order.push_back(i);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->slots[a].NC > b->slots[c].NC; });
+  std::vector<int4> grp[kGroups];
+  unsigned orders = 0;
   for (int i : order) {
     const BatchSlot& sl = b->slots[i];
-    for (int e0 = 0; e0 < sl.NC; e0 += sl.epb1) ct.push_back(make_int4(i, e0, std::min(sl.epb1, sl.NC - e0), sl.N));
-    for (int e0 = 0; e0 < sl.NC; e0 += sl.epb2) ct2.push_back(make_int4(i, e0, std::min(sl.epb2, sl.NC - e0), sl.N));
-    for (int e0 = 0; e0 < sl.NC; e0 += sl.epb) ct3.push_back(make_int4(i, e0, std::min(sl.epb, sl.NC - e0), sl.N));
-    for (int e0 = 0; e0 < sl.NC; e0 += sl.epbct) ct4.push_back(make_int4(i, e0, std::min(sl.epbct, sl.NC - e0), sl.N));
-    for (int t0 = 0; t0 < sl.nfp_faces; t0 += face_tile)
-      ft.push_back(make_int4(i, t0, std::min(face_tile, sl.nfp_faces - t0), sl.N));
-    smem[0] = std::max(smem[0], cell_smem_bytes(sl.N, sl.epb1, 0));
-    smem[1] = std::max(smem[1], cell_smem_bytes(sl.N, sl.epb2, 1));
-    smem[2] = std::max(smem[2], cell_smem_bytes(sl.N, sl.epb, 2));
-    smem[3] = std::max(smem[3], cell_smem_bytes(sl.N, sl.epbct, 3));
+    order_shape(b, sl);
+    const OrderShape& o = b->shape[sl.N];
+    orders |= 1u << sl.N;
+    auto cut = [&](int pass, int n, int step) {
+      for (int a = 0; a < n; a += step) grp[gidx(pass, sl.N)].push_back(make_int4(i, a, std::min(step, n - a), 0));
+    };
+    cut(PE1, sl.NC, o.epb[0]);
+    cut(PF1, sl.nfp_faces, kFaceTile);
+    // E2 chunks: one cell per thread where cells may skip their gradients, one group of
+    // epb cells where every cell needs them (as the single-solve launch)
+    const int chunk = sl.sd.skip ? o.threads[1] - o.threads[1] % o.epb[1] : o.epb[1];
+    cut(PE2, sl.NC, std::max(chunk, 1));
+    cut(PE3, sl.NC, o.epb[2]);
+    cut(PCT, sl.NC, o.epb[3]);
+    cut(PCTF, sl.nfp_two, kFaceTile);
   }
-  const int n_e1 = (int)ct.size(), n_e2 = (int)ct2.size(), n_e3 = (int)ct3.size(), n_ct = (int)ct4.size();
-  ct.insert(ct.end(), ct2.begin(), ct2.end());
-  ct.insert(ct.end(), ct3.begin(), ct3.end());
-  ct.insert(ct.end(), ct4.begin(), ct4.end());
+  std::vector<int4> ct, ft;
+  int cnt[kGroups], off[kGroups];
+  for (int g = 0; g < kGroups; g++) {
+    const int pass = g / (kMaxN + 1);
+    std::vector<int4>& dst = (pass == PF1 || pass == PCTF) ? ft : ct;
+    off[g] = (int)dst.size();
+    cnt[g] = (int)grp[g].size();
+    dst.insert(dst.end(), grp[g].begin(), grp[g].end());
+  }
   const int ns = (int)b->slots.size();
   if (ns > b->cap_solves || (int)ct.size() > b->cap_ctiles || (int)ft.size() > b->cap_ftiles) {
     int rc = batch_alloc(b, std::max(ns * 2, 16), std::max((int)ct.size() * 2, 1024), std::max((int)ft.size() * 2, 1024));
@@ -321,6 +373,8 @@ static int batch_rebuild(ChorusBatch* b) {
     rk_stage_records(sd[i], b->slots[i].dt, b->slots[i].k_stage, false, r);
     for (int k = 0; k < 5; k++) rk[(size_t)k * b->cap_solves + i] = r[k];
   }
+  std::vector<int> counts(cnt, cnt + kGroups);
+  counts.insert(counts.end(), off, off + kGroups);
   cudaError_t e = cudaSuccess;
   if (ns) e = cudaMemcpyAsync(b->d_solves, sd.data(), sizeof(SolveDev) * ns, cudaMemcpyHostToDevice, b->st);
   if (e == cudaSuccess && !ct.empty())
@@ -329,50 +383,78 @@ static int batch_rebuild(ChorusBatch* b) {
     e = cudaMemcpyAsync(b->d_ftiles, ft.data(), sizeof(int4) * ft.size(), cudaMemcpyHostToDevice, b->st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(b->d_rk, rk.data(), sizeof(RKStage) * rk.size(), cudaMemcpyHostToDevice, b->st);
-  int nt[5] = {n_e1, (int)ft.size(), n_e2, n_e3, n_ct};
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_ntiles, nt, sizeof nt, cudaMemcpyHostToDevice, b->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_gcount, counts.data(), sizeof(int) * counts.size(), cudaMemcpyHostToDevice, b->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
   if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch tables upload: %s", cudaGetErrorString(e));
-  b->ctiles = nt[3];
-  b->ftiles = nt[1];
+  int n3 = 0;
+  for (int N = kMinN; N <= kMaxN; N++) n3 += cnt[gidx(PE3, N)];
+  b->ctiles = n3;
+  b->ftiles = 0;
+  for (int N = kMinN; N <= kMaxN; N++) b->ftiles += cnt[gidx(PF1, N)];
+  // the graph launches one CTA per tile as captured; more tiles than that (a new order, or
+  // a larger composition) need a new capture, fewer leave CTAs that find no tile
   bool grew = false;
-  for (int p = 0; p < 4; p++) {
-    grew = grew || smem[p] > b->graph_smem[p];
-    b->smem[p] = std::max(b->smem[p], smem[p]);
+  for (int g = 0; g < kGroups; g++) {
+    b->cnt[g] = cnt[g];
+    grew = grew || cnt[g] > b->graph_grid[g];
   }
-  if (grew && b->graph) {
+  if (b->graph && grew) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
+  (void)orders;
   b->dirty = false;
   return CHORUS_OK;
 }
 
+// one step: for every order present, its own chain on its own stream -- five stages of
+// E1, F1, E2, E3, then the CT projection -- forked from and joined to the batch stream.
+// The orders' solves share nothing, so the chains run concurrently and the block
+// scheduler mixes their CTAs (FP64-bound flux passes of one order beside the integer
+// line operators of another); within a chain every launch is programmatic (scheduled
+// while its predecessor drains, waiting for it at entry).  Each launch has one CTA per
+// tile of the composition it was captured for.
 static void batch_enqueue_step(ChorusBatch* b) {
   BatchDev a;
   a.solves = b->d_solves;
   a.ctiles = b->d_ctiles;
   a.ftiles = b->d_ftiles;
-  a.ntiles = b->d_ntiles;
-  a.counters = b->d_counters;
+  a.gcount = b->d_gcount;
+  a.goff = b->d_gcount + kGroups;
   a.rk = b->d_rk;
   a.cap = b->cap_solves;
   a.pad = 0;
-  const size_t* sm = b->smem;
-  // every launch of the step has its own tile counter, so one memset per step clears
-  // them all; E1 starts each solve's wave-speed maximum; the launches are programmatic
-  // (each is scheduled while its predecessor drains and waits for it at entry)
-  cudaMemsetAsync(b->d_counters, 0, sizeof(int) * kCounterSlots, b->st);
-  for (int stage = 0; stage < 5; stage++) {
-    const int c0 = 4 * stage;
-    launch_pdl(kb_e1, b->grid_cells, 256, sm[0], b->st, a, c0, stage == 4 ? 3 : 1);
-    launch_pdl(kb_face, b->grid_faces, 128, 0, b->st, a, c0 + 1, 0);
-    launch_pdl(kb_e2, b->grid_cells, 256, sm[1], b->st, a, c0 + 2);  // also the face AV viscosities
-    launch_pdl(kb_e3, b->grid_cells, 128, sm[2], b->st, a, c0 + 3, stage);
+  cudaEventRecord(b->fork, b->st);
+  for (int N = kMaxN; N >= kMinN; N--) {
+    if (!b->shape[N].used) continue;
+    int any = 0;
+    for (int p = 0; p < kPasses; p++) any += b->cnt[gidx(p, N)];
+    if (!any) continue;
+    cudaStream_t st = b->side[N];
+    cudaStreamWaitEvent(st, b->fork, 0);
+    auto pass = [&](int p, int arg) {
+      const int g = gidx(p, N);
+      if (!b->cnt[g]) return;
+      PassShape ps = b->shape[N].pass[p];
+      ps.grid = b->cnt[g];
+      b->graph_grid[g] = ps.grid;
+#define CALL(n) launch_pass<n>(a, p, ps, st, arg)
+      CHORUS_BATCH_SWITCH(N, CALL)
+#undef CALL
+    };
+    for (int stage = 0; stage < 5; stage++) {
+      pass(PE1, stage == 4 ? 3 : 1);
+      pass(PF1, 0);
+      pass(PE2, 0);  // also the face AV viscosities
+      pass(PE3, stage);
+    }
+    pass(PCT, 0);
+    pass(PCTF, 0);
+    pass(PCT, 2);
+    cudaEventRecord(b->join[N], st);
+    cudaStreamWaitEvent(b->st, b->join[N], 0);
   }
-  launch_pdl(kb_ct, b->grid_cells, 128, sm[3], b->st, a, 20, 0);
-  launch_pdl(kb_face, b->grid_faces, 128, 0, b->st, a, 21, 2);
-  launch_pdl(kb_ct, b->grid_cells, 128, sm[3], b->st, a, 22, 2);
 }
 
 extern "C" {
@@ -384,21 +466,19 @@ int chorus_batch_create(int32_t device, ChorusBatch** out) {
   ChorusBatch* b = new ChorusBatch();
   b->device = device;
   cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_ntiles, sizeof(int) * 5);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_counters, sizeof(int) * kCounterSlots);
+  for (int N = kMinN; N <= kMaxN && e == cudaSuccess; N++) {
+    e = cudaStreamCreateWithFlags(&b->side[N], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[N], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_gcount, sizeof(int) * 2 * kGroups);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_gcount, 0, sizeof(int) * 2 * kGroups, b->st);
   if (e != cudaSuccess) {
     delete b;
     return set_err(CHORUS_ECUDA, "batch create: %s", cudaGetErrorString(e));
   }
   int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  b->grid_cells = sms * 8;  // persistent CTAs: 8 per SM (occupancy is not what bounds FP64)
-  b->grid_faces = sms * 8;
-  const int lim = 200 * 1024;
-  cudaFuncSetAttribute(kb_e1, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  cudaFuncSetAttribute(kb_e2, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  cudaFuncSetAttribute(kb_e3, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  cudaFuncSetAttribute(kb_ct, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && sms > 0) b->nsm = sms;
   int rc = batch_alloc(b, 16, 4096, 4096);
   if (rc) {
     delete b;
@@ -413,9 +493,14 @@ int chorus_batch_free(ChorusBatch* b) {
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->st);
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  void* ptrs[] = {b->d_solves, b->d_ctiles, b->d_ftiles, b->d_ntiles, b->d_counters, b->d_rk, b->d_eig, b->d_err};
+  void* ptrs[] = {b->d_solves, b->d_ctiles, b->d_ftiles, b->d_gcount, b->d_rk, b->d_eig, b->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (int N = kMinN; N <= kMaxN; N++) {
+    if (b->side[N]) cudaStreamDestroy(b->side[N]);
+    if (b->join[N]) cudaEventDestroy(b->join[N]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   cudaStreamDestroy(b->st);
   delete b;
   return CHORUS_OK;
@@ -430,17 +515,7 @@ int chorus_batch_add(ChorusBatch* b, ChorusCtx* ctx, int32_t* slot) {
   sl.N = sl.sd.N;
   sl.NC = sl.sd.NC;
   sl.nfp_faces = (sl.sd.nface2 + sl.sd.nface1) * sl.N;
-  // tiles keep the cells-per-thread ratio of the solve's tuned shapes at the batched
-  // kernels' fixed CTA sizes (E1, E2 256 threads, E3 128); E1 and E2 tiles of at most 8
-  // cells keep their shared memory (and occupancy) in the range the shapes were tuned for
-  auto scaled = [&](int pass, int threads, int cap) {
-    const int e = ctx_epb(ctx, pass) * threads / std::max(ctx_threads(ctx, pass), 1);
-    return std::max(1, std::min(e, cap));
-  };
-  sl.epb = scaled(2, 128, 64);
-  sl.epb1 = scaled(0, 256, 8);
-  sl.epb2 = scaled(1, 256, 8);
-  sl.epbct = std::max(1, std::min(ctx_epb(ctx, 3), 64));
+  sl.nfp_two = sl.sd.nface2 * sl.N;
   sl.dt = ctx_dt(ctx);
   sl.k_stage = ctx_kstage(ctx);
   sl.active = true;
@@ -480,12 +555,12 @@ int chorus_batch_step(ChorusBatch* b, int32_t nsteps) {
     cudaGraph_t g;
     cudaError_t e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "capture: %s", cudaGetErrorString(e));
+    for (int i = 0; i < kGroups; i++) b->graph_grid[i] = 0;
     batch_enqueue_step(b);
     e = cudaStreamEndCapture(b->st, &g);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
     if (e == cudaSuccess) cudaGraphDestroy(g);
     if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch graph: %s", cudaGetErrorString(e));
-    for (int p = 0; p < 4; p++) b->graph_smem[p] = b->smem[p];
   }
   for (int s = 0; s < nsteps; s++) {
     cudaError_t e = cudaGraphLaunch(b->graph, b->st);

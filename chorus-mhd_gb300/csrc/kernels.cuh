@@ -628,16 +628,13 @@ __device__ __forceinline__ bool needs_gradients(const SolveDev& s, int c) {
   return (b.x >= 0 && s.nv[b.x]) || (b.y >= 0 && s.nv[b.y]) || (b.z >= 0 && s.nv[b.z]) || (b.w >= 0 && s.nv[b.w]);
 }
 
-// E2 over a chunk of `chunk` (<= blockDim.x) cells per CTA: every thread tests one
-// cell, the CTA compacts the cells that need gradients into an ordered list and runs
+// E2 over a chunk of `chunk` (<= blockDim.x) cells starting at c0: every thread tests
+// one cell, the CTA compacts the cells that need gradients into an ordered list and runs
 // them in groups of epb, so chunks without viscous work cost one coalesced test
-template <int N>
-__global__ void __launch_bounds__(512) k_e2(SolveDev s, int epb, int chunk) {
-  extern __shared__ __align__(16) double sm[];
-  pdl_wait();
+template <int N, class O>
+__device__ __forceinline__ void e2_chunk(const SolveDev& s, int c0, int chunk, int epb, double* sm) {
   __shared__ int list[512];
   __shared__ int woff[17];
-  const int c0 = blockIdx.x * chunk;
   const int c = c0 + threadIdx.x;
   const bool mine = (int)threadIdx.x < chunk && c < s.NC;
   if (mine) cell_face_mu<N>(s, c);
@@ -655,9 +652,16 @@ __global__ void __launch_bounds__(512) k_e2(SolveDev s, int epb, int chunk) {
   const int n = woff[blockDim.x >> 5];
   __syncthreads();
   for (int g = 0; g < n; g += epb) {
-    e2_cells<N, OpsTU>(s, list + g, min(epb, n - g), sm);
+    e2_cells<N, O>(s, list + g, min(epb, n - g), sm);
     __syncthreads();
   }
+}
+
+template <int N>
+__global__ void __launch_bounds__(512) k_e2(SolveDev s, int epb, int chunk) {
+  extern __shared__ __align__(16) double sm[];
+  pdl_wait();
+  e2_chunk<N, OpsTU>(s, blockIdx.x * chunk, chunk, epb, sm);
 }
 // ---------------------------------------------------------------------------
 // F2: face-averaged gradients and face AV viscosity
