@@ -516,6 +516,66 @@ def run_serving(args, device, tmp):
     return out
 
 
+def run_serving_mix(args):
+    """The serving configuration on its stated mix: Poisson arrivals of solves drawn from
+    the batched configuration's population (cells per side log-uniform on 32..256, N in
+    3..6, Orszag-Tang / rotor / Alfven, rotor sides raised to 192 points), end times
+    U(0.1, 1.0), admitted under a 120 GB budget, served by continuous batching and by the
+    plain sequential loop.  Each stream has the same `--serving-requests` requests (same
+    cases and end times at every rate; only the arrival times scale with the rate).  A
+    request averages about ten seconds of GPU work with a tail of minutes, so at every
+    stated rate (10-500 per second) a stream's requests have all arrived long before the
+    first large ones finish: the run is bounded by the requests, not the rates.  One more
+    batched stream runs under a budget of a few of its largest solves, so that admission
+    waits for memory."""
+    import numpy as np
+    import torch
+    from chorus_mhd import Mesh, _lib, ensemble, serve
+    torch.cuda.set_device(0)
+    tmp = tempfile.mkdtemp(prefix="chorus_c5_")
+    pool = ensemble.draw(count=256)
+    rng = np.random.default_rng(5)
+    picks = rng.integers(0, len(pool), args.serving_requests)
+    ends = rng.uniform(0.1, 1.0, args.serving_requests)
+    dirs = {}
+    for i in sorted(set(int(p) for p in picks)):
+        dirs[i] = ensemble.write_all([pool[i]], os.path.join(tmp, "case%03d" % i))[0]
+    sizes = {}
+    steps_total, work = 0, 0.0
+    for i, e in zip(picks, ends):
+        m = Mesh(dirs[int(i)])
+        sizes[int(i)] = int(_lib.load().chorus_mesh_device_bytes(m._h))
+        k = int(math.ceil(e / m.params.dt - 1e-9))
+        steps_total += k
+        work += 5.0 * m.ncell * m.N * m.N * k
+        m.close()
+    budget = 120 * 10 ** 9
+    arrivals = np.cumsum(np.random.default_rng(6).exponential(1.0, args.serving_requests))
+    out = {"metric": "p50/p99 time-to-solution (s) and throughput, serving stream", "impl": "chorus",
+           "config": {"workload": "serving: Poisson arrivals of the 256-solve population (sides 32-256 log-uniform, "
+                                  "N 3-6, Orszag-Tang/rotor/Alfven), end times U(0.1,1.0), 120 GB budget",
+                      "requests_per_stream": args.serving_requests, "dof_stage_work": work, "steps": steps_total,
+                      "largest_request_bytes": max(sizes.values())},
+           "rates": {}}
+    serve.serve([(dirs[int(picks[0])], 0.0, 0.001)], mode="batched")  # warm-up
+    for rate in args.serving_rates:
+        reqs = [(dirs[int(p)], float(a / rate), float(e)) for p, a, e in zip(picks, arrivals, ends)]
+        rb, mb = serve.serve(reqs, mode="batched", hbm_budget_bytes=budget)
+        rs, ms = serve.serve(reqs, mode="sequential")
+        b, q = serve.summarize(rb, mb), serve.summarize(rs, ms)
+        out["rates"][str(rate)] = {"batched": b, "sequential": q,
+                                   "throughput_ratio": b["throughput_dof_stage_per_s"] / max(q["throughput_dof_stage_per_s"], 1e-30),
+                                   "p99_ratio_sequential_over_batched": q["p99_latency_s"] / max(b["p99_latency_s"], 1e-30)}
+        print(json.dumps({"rate": rate, **out["rates"][str(rate)]}), flush=True)
+    out["budget_binds_at_120GB"] = any(v["batched"]["waited_for_memory"] for v in out["rates"].values())
+    small = 3 * max(sizes.values())
+    rate = max(args.serving_rates)
+    reqs = [(dirs[int(p)], float(a / rate), float(e)) for p, a, e in zip(picks, arrivals, ends)]
+    rb, mb = serve.serve(reqs, mode="batched", hbm_budget_bytes=small)
+    out["small_budget"] = {"hbm_budget_bytes": small, "rate": rate, "batched": serve.summarize(rb, mb)}
+    print(json.dumps(out), flush=True)
+
+
 # per element per RK stage, from ncu on the four stage kernels (Orszag-Tang 262x262,
 # N=5, after the warm-up steps): FP64 thread instructions (DFMA + DADD + DMUL) and flops
 # (2*DFMA + DADD + DMUL); DRAM bytes read + written.  FP64_FORM_... is the count of the
@@ -643,9 +703,10 @@ def run_reference(args):
 def main():
     global NX, N_SOL, JITTER, SEED, PROBLEM, MU, ETA0, WORKLOAD
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="C2", choices=sorted(WORKLOADS),
+    ap.add_argument("--workload", default="C2", choices=sorted(WORKLOADS) + ["C5"],
                     help="C2: Orszag-Tang 512^2 jittered N=5 (default); C1: Orszag-Tang 64^2 N=4; "
-                         "C3: rotor 256^2 jittered N=4, FREE boundaries")
+                         "C3: rotor 256^2 jittered N=4, FREE boundaries; C5: the serving stream on its "
+                         "stated mix (its own JSON line)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
@@ -668,6 +729,9 @@ def main():
     ap.add_argument("--mu", type=float, default=0.0, help="physical viscosity (the configurations use 0)")
     ap.add_argument("--eta0", type=float, default=0.0, help="resistivity (the configurations use 0)")
     args = ap.parse_args()
+    if args.workload == "C5":
+        run_serving_mix(args)
+        return
     MU, ETA0 = args.mu, args.eta0
     WORKLOAD = args.workload
     if args.run_steps:

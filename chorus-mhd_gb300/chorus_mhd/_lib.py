@@ -34,7 +34,7 @@ class ChorusServeRequest(ctypes.Structure):
 
 class ChorusServeConfig(ctypes.Structure):
     _fields_ = [("device", c_int), ("mode", c_int), ("hbm_budget_bytes", ctypes.c_int64), ("max_active", c_int),
-                ("pad", c_int)]
+                ("gpu_setup", c_int)]
 
 
 class ChorusServeResult(ctypes.Structure):
@@ -96,6 +96,7 @@ SIGNATURES = {
     "chorus_serve_run": (c_int, [P(ChorusServeRequest), c_int, P(ChorusServeConfig), P(ChorusServeResult), dp]),
     "chorus_mesh_device_bytes": (ctypes.c_int64, [c_void_p]),
     "chorus_mesh_load": (c_int, [c_char_p, P(c_void_p)]),
+    "chorus_mesh_load_gpu": (c_int, [c_char_p, c_int, P(c_void_p)]),
     "chorus_mesh_free": (c_int, [c_void_p]),
     "chorus_mesh_output_info": (c_int, [c_void_p, ip, ip]),
     "chorus_plot_create": (c_int, [c_void_p, ip, ip, dp, dp, c_int, c_int, dp, c_int, P(c_void_p)]),

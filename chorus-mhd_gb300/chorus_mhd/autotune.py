@@ -7,7 +7,8 @@ sweeps the cells per CTA ("epb") and threads per CTA, timing the pass with CUDA 
 exact-zero viscous skipping off, i.e. on its full work.  Results are cached per GPU
 model in a JSON file (``~/.cache/chorus_gb300/tune_<gpu>.json`` unless
 ``CHORUS_TUNE_FILE`` names one) and applied by ``apply`` to any bound ``Solver``; the
-batched form takes each solve's E3 shape as its tile size.
+batched form launches each order's passes with the shapes of the first solve of that
+order it holds.
 
     python -m chorus_mhd.autotune            # tune N = 3..6 and write the cache
 """

@@ -29,13 +29,14 @@ def poisson_requests(rate: float, count: int, case_dirs: list[str], seed: int = 
     return [(case_dirs[int(p)], float(a), float(e)) for p, a, e in zip(picks, t, ends)]
 
 
-def serve(requests, mode: str = "batched", hbm_budget_bytes: int = 0, device: int = 0, max_active: int = 0):
+def serve(requests, mode: str = "batched", hbm_budget_bytes: int = 0, device: int = 0, max_active: int = 0,
+          gpu_setup: bool = False):
     """Run the request loop; returns (per-request dicts, makespan seconds).
 
     A request is (case_dir, arrival_s, end_time) or (case_dir, arrival_s, end_time, out)
     where out may hold "Q" (a contiguous float64 array of the solve's 9*N*N*NCELL doubles,
     filled with the final state) and "restart" (a path that receives the final state as a
-    restart stream)."""
+    restart stream).  gpu_setup builds each request's maps and geometry on the device."""
     L = _lib.load()
     n = len(requests)
     arr = (ChorusServeRequest * n)()
@@ -60,7 +61,8 @@ def serve(requests, mode: str = "batched", hbm_budget_bytes: int = 0, device: in
             keep.append(rb)
             arr[i].restart_path = rb
     cfg = ChorusServeConfig(device=device, mode=1 if mode == "sequential" else 0,
-                            hbm_budget_bytes=int(hbm_budget_bytes), max_active=int(max_active), pad=0)
+                            hbm_budget_bytes=int(hbm_budget_bytes), max_active=int(max_active),
+                            gpu_setup=1 if gpu_setup else 0)
     out = (ChorusServeResult * n)()
     mk = ctypes.c_double()
     check(L.chorus_serve_run(arr, n, ctypes.byref(cfg), out, ctypes.byref(mk)))

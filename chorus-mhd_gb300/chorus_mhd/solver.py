@@ -28,12 +28,18 @@ def _ip(a: np.ndarray):
 
 
 class Mesh:
-    """The reference's setup chain for one case directory (readinput ... calcjacob)."""
+    """The reference's setup chain for one case directory (readinput ... calcjacob).
 
-    def __init__(self, case_dir: str):
+    With `device` given, the maps and the geometry are built on that GPU
+    (chorus_mesh_load_gpu; the same arrays bit for bit)."""
+
+    def __init__(self, case_dir: str, device: int | None = None):
         self.L = _lib.load()
         h = ctypes.c_void_p()
-        check(self.L.chorus_mesh_load(case_dir.encode(), ctypes.byref(h)))
+        if device is None:
+            check(self.L.chorus_mesh_load(case_dir.encode(), ctypes.byref(h)))
+        else:
+            check(self.L.chorus_mesh_load_gpu(case_dir.encode(), int(device), ctypes.byref(h)))
         self._h = h
         self.case_dir = case_dir
         self.dims = ChorusDims()

@@ -1273,6 +1273,20 @@ int chorus_mesh_load(const char* dir, ChorusMesh** out) {
   return CHORUS_OK;
 }
 
+int chorus_mesh_load_gpu(const char* dir, int32_t device, ChorusMesh** out) {
+  if (!dir || !out) return set_err(CHORUS_EINVAL, "null argument");
+  *out = nullptr;
+  ChorusMesh* mh = new ChorusMesh();
+  std::string err;
+  int rc = mesh_load_gpu(dir, device, mh->m, err);
+  if (rc) {
+    delete mh;
+    return set_err(rc, "%s", err.c_str());
+  }
+  *out = mh;
+  return CHORUS_OK;
+}
+
 int chorus_mesh_output_info(const ChorusMesh* mh, int32_t* nre, int32_t* nwrite) {
   if (!mh) return set_err(CHORUS_EINVAL, "null mesh");
   if (nre) *nre = mh->m.nre;

@@ -26,6 +26,23 @@ struct Mesh {
 };
 
 int mesh_load(const std::string& dir, Mesh& m, std::string& err);
+// the same with the map building and the geometry on a GPU (meshgpu.cu): bit-identical
+// results; a mesh the device path finds invalid is rebuilt on the host for the error
+int mesh_load_gpu(const std::string& dir, int device, Mesh& m, std::string& err);
+
+// stages of the setup chain shared by both paths (mesh.cpp)
+struct BndRecord {      // one record of the .BND file whose vertices are on this partition
+  int line;             // 1-based record number
+  int a, b;             // local vertex ids of the edge
+  int kind;             // 1 CYCL, 2 FREE, 0 anything else (rejected when its face is found)
+  std::string type;
+};
+int mesh_parse(const std::string& dir, Mesh& m, std::vector<BndRecord>& bnd, std::string& err);
+int mesh_maps_host(Mesh& m, const std::vector<BndRecord>& bnd, std::string& err);
+int boundary_face(Mesh& m, const BndRecord& r, int K, std::vector<char>& bflag, std::string& err);
+int mesh_periodic(Mesh& m, std::string& err);
+void mesh_operators(Mesh& m);
+void mesh_geometry_host(Mesh& m);
 void setsandpoints(int np, double* xs, double* xf);
 double lagrange(const double* x, int n, int i, double xv);
 void compute_L_M(int N, const double* Xs, const double* Xf, double* L, double* M);

@@ -146,7 +146,9 @@ const int kIVFACE[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};  // connectivity.f90
 
 }  // namespace
 
-int mesh_load(const std::string& dir, Mesh& m, std::string& err) {
+// QUAD.INP, the cell and vertex files with GLOB2LOCAL, and the boundary file's records
+// (readinput.f90:6-36, readGRIDinfo.f90:1-259)
+int mesh_parse(const std::string& dir, Mesh& m, std::vector<BndRecord>& bnd, std::string& err) {
   // ---- QUAD.INP (readinput.f90:6-36) + extension block
   std::vector<std::string> L;
   if (read_lines(dir + "/QUAD.INP", L) || L.size() < 29) {
@@ -226,6 +228,28 @@ int mesh_load(const std::string& dir, Mesh& m, std::string& err) {
       m.IVCELL[ic + (size_t)nglob * k] = g2l[g];
     }
   m.NVERT = (int)m.XV.size();
+  // ---- boundary file (readGRIDinfo.f90:201-259): records on this partition, in order
+  std::vector<std::string> B;
+  read_lines(dir + "/" + nbnd, B);
+  bnd.clear();
+  for (size_t i = 0; i < B.size(); i++) {
+    int ib, a, b, reg, pat;
+    char ty[64] = {0};
+    if (std::sscanf(B[i].c_str(), "%d %d %d %d %d %63s", &ib, &a, &b, &reg, &pat, ty) != 6) {
+      err = "bad boundary line " + std::to_string(i + 1);
+      return CHORUS_EIO;
+    }
+    std::string t(ty);
+    t.erase(std::remove(t.begin(), t.end(), '\''), t.end());
+    t.erase(std::remove(t.begin(), t.end(), '"'), t.end());
+    if (a < 1 || a > nvg || b < 1 || b > nvg || !g2l[a] || !g2l[b]) continue;  // not on this partition
+    bnd.push_back(BndRecord{(int)i + 1, g2l[a], g2l[b], t == "CYCL" ? 1 : (t == "FREE" ? 2 : 0), t});
+  }
+  return CHORUS_OK;
+}
+
+// CHECK_MESH, CONNECTIVITY and CONNECT_BDRY's boundary lists on the host
+int mesh_maps_host(Mesh& m, const std::vector<BndRecord>& bnd, std::string& err) {
   const int NC = m.NCELL;
   auto ivcell = [&](int ic, int k) { return m.IVCELL[ic + (size_t)NC * k]; };
 
@@ -295,42 +319,43 @@ int mesh_load(const std::string& dir, Mesh& m, std::string& err) {
     m.IF2V[f + (size_t)NF] = f_v2[f];
   }
 
-  // ---- boundary file (readGRIDinfo.f90:201-259) and CONNECT_BDRY
-  std::vector<std::string> B;
-  read_lines(dir + "/" + nbnd, B);
+  // ---- CONNECT_BDRY: boundary faces in .BND order
   std::vector<char> bflag(NF, 0);
   m.IBFCYC.clear();
   m.IBFREE.clear();
-  for (size_t i = 0; i < B.size(); i++) {
-    int ib, a, b, reg, pat;
-    char ty[64] = {0};
-    if (std::sscanf(B[i].c_str(), "%d %d %d %d %d %63s", &ib, &a, &b, &reg, &pat, ty) != 6) {
-      err = "bad boundary line " + std::to_string(i + 1);
-      return CHORUS_EIO;
-    }
-    std::string t(ty);
-    t.erase(std::remove(t.begin(), t.end(), '\''), t.end());
-    t.erase(std::remove(t.begin(), t.end(), '"'), t.end());
-    if (a < 1 || a > nvg || b < 1 || b > nvg || !g2l[a] || !g2l[b]) continue;  // not on this partition
-    auto it = edges.find(edge_key(g2l[a], g2l[b]));
-    if (it == edges.end()) { err = "boundary edge " + std::to_string(i + 1) + " is not a cell face"; return CHORUS_EMESH; }
-    if (it->second.second >= 0) { err = "boundary edge " + std::to_string(i + 1) + " is an interior face"; return CHORUS_EMESH; }
+  for (const BndRecord& r : bnd) {
+    auto it = edges.find(edge_key(r.a, r.b));
+    if (it == edges.end()) { err = "boundary edge " + std::to_string(r.line) + " is not a cell face"; return CHORUS_EMESH; }
+    if (it->second.second >= 0) { err = "boundary edge " + std::to_string(r.line) + " is an interior face"; return CHORUS_EMESH; }
     int code = it->second.first;
     int K = m.IC2F[(code / 4) + (size_t)NC * (code % 4)];
-    bflag[K - 1] = 1;
-    if (t == "CYCL") m.IBFCYC.push_back(K);
-    else if (t == "FREE") m.IBFREE.push_back(K);
-    else {
-      err = "boundary type " + t + " has no flux routine in the reference (bcflux.f90 handles FREE only)";
-      return CHORUS_EMESH;
-    }
+    int rc = boundary_face(m, r, K, bflag, err);
+    if (rc) return rc;
   }
   m.IBFINTER.clear();
   for (int f = 0; f < NF; f++) {
     if (m.IF2C[f + (size_t)NF]) m.IBFINTER.push_back(f + 1);
     else if (!bflag[f]) { err = "boundary face " + std::to_string(f + 1) + " is missing from the BND file"; return CHORUS_EMESH; }
   }
+  return CHORUS_OK;
+}
 
+// one boundary record whose face K (1-based) was found: its list by type (shared by the
+// host and device setup paths, so both report the same errors in the same order)
+int boundary_face(Mesh& m, const BndRecord& r, int K, std::vector<char>& bflag, std::string& err) {
+  bflag[K - 1] = 1;
+  if (r.kind == 1) m.IBFCYC.push_back(K);
+  else if (r.kind == 2) m.IBFREE.push_back(K);
+  else {
+    err = "boundary type " + r.type + " has no flux routine in the reference (bcflux.f90 handles FREE only)";
+    return CHORUS_EMESH;
+  }
+  return CHORUS_OK;
+}
+
+// MAPCYCLOC: periodic partners on the host (the list is the domain's perimeter)
+int mesh_periodic(Mesh& m, std::string& err) {
+  const int NF = m.NFACE;
   // ---- periodic faces: midpoint matching (connect_bdry.f90:275-314, map_cyc_loc.f90:1-42)
   const int NCY = (int)m.IBFCYC.size();
   std::vector<double> mx(NCY), my(NCY);
@@ -385,7 +410,11 @@ int mesh_load(const std::string& dir, Mesh& m, std::string& err) {
   m.CYC2FPAIR.resize(2 * (size_t)m.NPAIR);
   for (int p = 0; p < m.NPAIR; p++) { m.CYC2FPAIR[p] = p1[p]; m.CYC2FPAIR[p + m.NPAIR] = p2[p]; }
 
-  // ---- SD operators and geometry
+  return CHORUS_OK;
+}
+
+// setsandpoints, computeLandM and face2fpconnec (initsetup.f90:167-379)
+void mesh_operators(Mesh& m) {
   const int N = m.N;
   m.Xs.assign(N, 0.0);
   m.Xf.assign(N + 1, 0.0);
@@ -401,6 +430,13 @@ int mesh_load(const std::string& dir, Mesh& m, std::string& err) {
     m.iface2fp[nfp - 1 + 2 * N] = N - nfp + 1; m.jface2fp[nfp - 1 + 2 * N] = N + 1;
     m.iface2fp[nfp - 1 + 3 * N] = 1;         m.jface2fp[nfp - 1 + 3 * N] = N - nfp + 1;
   }
+}
+
+// mapder + calcjacob (mapder.f90:1-76, calcjacob.f90:1-86) and xyCoor_atGps
+// (mapder.f90:255-273) on the host
+void mesh_geometry_host(Mesh& m) {
+  const int N = m.N, NC = m.NCELL;
+  auto ivcell = [&](int ic, int k) { return m.IVCELL[ic + (size_t)NC * k]; };
   const size_t ns = (size_t)N * N * NC, nf1 = (size_t)(N + 1) * N * NC;
   m.Jac.assign(ns, 0.0);
   m.S1.assign(4 * nf1, 0.0);
@@ -449,7 +485,17 @@ int mesh_load(const std::string& dir, Mesh& m, std::string& err) {
         }
       }
   }
-  m.params.NCELLGLOB = NC;
+}
+
+int mesh_load(const std::string& dir, Mesh& m, std::string& err) {
+  std::vector<BndRecord> bnd;
+  int rc = mesh_parse(dir, m, bnd, err);
+  if (!rc) rc = mesh_maps_host(m, bnd, err);
+  if (!rc) rc = mesh_periodic(m, err);
+  if (rc) return rc;
+  mesh_operators(m);
+  mesh_geometry_host(m);
+  m.params.NCELLGLOB = m.NCELL;
   return CHORUS_OK;
 }
 

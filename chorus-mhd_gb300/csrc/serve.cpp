@@ -49,9 +49,9 @@ void wait_until(std::chrono::steady_clock::time_point t0, double t) {
   if (d > 0) std::this_thread::sleep_for(std::chrono::duration<double>(d));
 }
 
-int open_request(const ChorusServeRequest& r, int device, Live& L, int64_t* dof, int32_t* steps, double* ctime) {
-  (void)device;
-  int rc = chorus_mesh_load(r.case_dir, &L.mesh);
+int open_request(const ChorusServeRequest& r, int device, int gpu_setup, Live& L, int64_t* dof, int32_t* steps,
+                 double* ctime) {
+  int rc = gpu_setup ? chorus_mesh_load_gpu(r.case_dir, device, &L.mesh) : chorus_mesh_load(r.case_dir, &L.mesh);
   if (rc) return rc;
   ChorusDims d;
   ChorusParams p;
@@ -108,7 +108,7 @@ extern "C" int chorus_serve_run(const ChorusServeRequest* reqs, int32_t n, const
       int32_t steps = 0;
       double ctime_end = 0.0;
       out[i].admit_s = now_s(t0);
-      int rc = open_request(reqs[i], dev, L, &dof, &steps, &ctime_end);
+      int rc = open_request(reqs[i], dev, cfg->gpu_setup, L, &dof, &steps, &ctime_end);
       if (!rc) rc = chorus_gpu_bind_mesh(L.mesh, dev, &L.ctx);
       if (!rc) rc = chorus_initial_state(L.mesh, L.ctx, nullptr);
       if (!rc) rc = chorus_gpu_set_option(L.ctx, "diagnostics", 0);
@@ -157,7 +157,7 @@ extern "C" int chorus_serve_run(const ChorusServeRequest* reqs, int32_t n, const
         double ctime_end = 0.0;
         pending = Live();
         pending.req = next;
-        rc = open_request(reqs[next], dev, pending, &dof, &steps, &ctime_end);
+        rc = open_request(reqs[next], dev, cfg->gpu_setup, pending, &dof, &steps, &ctime_end);
         out[next].dof = dof;
         out[next].steps = steps;
         out[next].ctime = ctime_end;

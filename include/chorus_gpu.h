@@ -292,7 +292,8 @@ typedef struct ChorusServeConfig {
   int32_t mode;              /* 0 continuous batching, 1 plain sequential */
   int64_t hbm_budget_bytes;  /* 0 = no limit */
   int32_t max_active;        /* 0 = no limit */
-  int32_t pad;
+  int32_t gpu_setup;         /* 1: build each request's maps and geometry on the device
+                                (chorus_mesh_load_gpu), 0: on the host */
 } ChorusServeConfig;
 typedef struct ChorusServeResult {
   double admit_s, finish_s, latency_s; /* seconds since start; latency = finish - arrival */
@@ -316,6 +317,13 @@ int64_t chorus_mesh_device_bytes(const ChorusMesh* mesh);
  * reference's; the geometry follows its evaluation order.
  * --------------------------------------------------------------------------- */
 int chorus_mesh_load(const char* case_dir, ChorusMesh** mesh);
+/* chorus_mesh_load with the map building and the geometry on `device`: the files are
+ * parsed on the host; CHECK_MESH, CONNECTIVITY (an edge hash table and a scan give the
+ * reference's face numbering), the boundary lookups, IBFINTER and mapder/calcjacob run
+ * as kernels, MAPCYCLOC on the host.  Every array is bit-identical to chorus_mesh_load's;
+ * a mesh the kernels find invalid is rebuilt on the host, which returns the reference's
+ * error for it.  Allocates and frees temporary device memory. */
+int chorus_mesh_load_gpu(const char* case_dir, int32_t device, ChorusMesh** mesh);
 int chorus_mesh_free(ChorusMesh* mesh);
 /* dims/params as read; *maxiter = MAXITER, *problem = 0 OT, 1 rotor, 2 Alfven. */
 int chorus_mesh_info(const ChorusMesh* mesh, ChorusDims* dims, ChorusParams* params, int32_t* maxiter,
