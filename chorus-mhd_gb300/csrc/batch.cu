@@ -183,6 +183,12 @@ static void pass_shapes(int nsm, const int (&epb)[4], const int (&threads)[4], P
   cudaFuncSetAttribute(kg_e2<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   cudaFuncSetAttribute(kg_e3<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   cudaFuncSetAttribute(kg_ct<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  // every pass kernel asks for the same shared-memory carveout, so that CTAs of the
+  // concurrent order chains share an SM without reconfiguring it
+  const void* fns[6] = {(const void*)kg_e1<N>, (const void*)kg_f1<N>, (const void*)kg_e2<N>,
+                        (const void*)kg_e3<N>, (const void*)kg_ct<N>, (const void*)kg_ctface<N>};
+  for (const void* f : fns)
+    cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   auto fill = [&](PassShape& p, const void* fn, int thr, int e, size_t smem) {
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, thr, smem) != cudaSuccess || occ < 1) occ = 1;
@@ -331,6 +337,11 @@ static int batch_rebuild(ChorusBatch* b) {
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->slots[a].NC > b->slots[c].NC; });
   std::vector<int4> grp[kGroups];
   unsigned orders = 0;
+  // E2 chunks as the single-solve launch sizes them: up to one cell per thread, but small
+  // enough for about 16 CTAs per SM over all the order's cells, so that small solves whose
+  // cells all need gradients spread over the GPU
+  long long order_cells[kMaxN + 1] = {0};
+  for (int i : order) order_cells[b->slots[i].N] += b->slots[i].NC;
   for (int i : order) {
     const BatchSlot& sl = b->slots[i];
     order_shape(b, sl);
@@ -341,10 +352,11 @@ static int batch_rebuild(ChorusBatch* b) {
     };
     cut(PE1, sl.NC, o.epb[0]);
     cut(PF1, sl.nfp_faces, kFaceTile);
-    // E2 chunks: one cell per thread where cells may skip their gradients, one group of
-    // epb cells where every cell needs them (as the single-solve launch)
-    const int chunk = sl.sd.skip ? o.threads[1] - o.threads[1] % o.epb[1] : o.epb[1];
-    cut(PE2, sl.NC, std::max(chunk, 1));
+    long long chunk = order_cells[sl.N] / (16LL * b->nsm);
+    chunk = std::max<long long>(o.epb[1], std::min<long long>(chunk, o.threads[1]));
+    chunk -= chunk % o.epb[1];
+    if (!sl.sd.skip) chunk = o.epb[1];
+    cut(PE2, sl.NC, (int)std::max<long long>(chunk, 1));
     cut(PE3, sl.NC, o.epb[2]);
     cut(PCT, sl.NC, o.epb[3]);
     cut(PCTF, sl.nfp_two, kFaceTile);
@@ -528,6 +540,13 @@ int chorus_batch_add(ChorusBatch* b, ChorusCtx* ctx, int32_t* slot) {
     b->slots.push_back(sl);
   } else {
     b->slots[idx] = sl;
+  }
+  // a reused slot starts without the error flag a previous solve in it may have raised
+  // (a slot beyond the tables' capacity gets cleared flags when they grow)
+  if (idx < b->cap_solves) {
+    cudaError_t e = cudaMemsetAsync(b->d_err + idx, 0, sizeof(unsigned int), b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) return set_err(CHORUS_ECUDA, "batch add: %s", cudaGetErrorString(e));
   }
   b->dirty = true;
   if (slot) *slot = idx;

@@ -62,26 +62,32 @@ __host__ __device__ __forceinline__ double times_sign(double x, double s) {
 }
 
 // Contravariant ideal-MHD flux F*sx + G*sy of getIfluxvectors (getrusanov.f90:111-153)
-// as used by inviscid_flux_interior (compflux.f90:77-78, 96-97).
+// as used by inviscid_flux_interior (compflux.f90:77-78, 96-97).  Written in the
+// momenta: with m = (ru, rv, rw), the mass flux m.s, the normal velocity (m.s)/rho and
+// the normal field over rho, Bn/rho, give every term without forming u, v, w
+// (u*Bn = ru*(Bn/rho), u.B = (m.B)/rho, rho|u|^2 = |m|^2/rho), 40 FP64 operations.
 __host__ __device__ __forceinline__ void iflux_contra(const double* q, double sx, double sy, double gm1,
                                                       double* F) {
   const double rho = q[0], ru = q[1], rv = q[2], rw = q[3], E = q[4], Bx = q[5], By = q[6], Bz = q[7];
   const double ri = rcp_pos(rho);
-  const double u = ru * ri, v = rv * ri, w = rw * ri;
-  const double B2 = Bx * Bx + By * By + Bz * Bz;
-  const double ke = ru * u + rv * v + rw * w;
-  const double pg = gm1 * (E - 0.5 * ke - 0.5 * B2);
-  const double pt = pg + 0.5 * B2;
-  const double Un = u * sx + v * sy;
+  const double F0 = ru * sx + rv * sy;  // rho * Un
+  const double Un = F0 * ri;
   const double Bn = Bx * sx + By * sy;
-  F[0] = ru * sx + rv * sy;
+  const double bn = Bn * ri;            // Bn / rho
+  const double B2 = Bx * Bx + By * By + Bz * Bz;
+  const double m2 = ru * ru + rv * rv + rw * rw;
+  const double hB2 = half(B2);
+  const double pg = gm1 * (E - half(m2) * ri - hB2);
+  const double pt = pg + hB2;
+  const double mB = ru * Bx + rv * By + rw * Bz;
+  F[0] = F0;
   F[1] = ru * Un + pt * sx - Bx * Bn;
   F[2] = rv * Un + pt * sy - By * Bn;
   F[3] = rw * Un - Bz * Bn;
-  F[4] = (E + pt) * Un - (u * Bx + v * By + w * Bz) * Bn;
-  F[5] = Bx * Un - u * Bn;
-  F[6] = By * Un - v * Bn;
-  F[7] = Bz * Un - w * Bn;
+  F[4] = (E + pt) * Un - mB * bn;
+  F[5] = Bx * Un - ru * bn;
+  F[6] = By * Un - rv * bn;
+  F[7] = Bz * Un - rw * bn;
 }
 
 // Rusanov flux of getrusanovflux (getrusanov.f90:1-109) along the unit normal (ux,uy),

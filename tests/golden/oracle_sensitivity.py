@@ -1,6 +1,6 @@
 """How far two correct FP64 evaluations of the same scheme drift apart over a long run.
 
-    python tests/golden/oracle_sensitivity.py NAME [--threads T] [--perturb-ulp SEED]
+    python tests/golden/oracle_sensitivity.py NAME [--threads T] [--perturb-ulp SEED] [--record]
 
 Builds a second copy of the oracle that differs from the committed one only in its
 floating-point contraction (gcc -ffp-contract=fast, plus -mfma on x86-64: a*b+c becomes
@@ -15,6 +15,9 @@ below which no FP64 implementation that is not bit-identical to the reference ca
 With --perturb-ulp the committed oracle itself runs instead, from its initial state with
 every value moved by one unit in the last place up or down (seeded signs): the growth of
 a one-ulp perturbation of the state under the scheme, with no difference in arithmetic.
+
+--record keeps the curve in tests/golden/NAME_sensitivity.npz (key "contracted" or
+"ulp<SEED>": rows of checkpoint, estimated relative L2), beside the fixture it measures.
 """
 from __future__ import annotations
 
@@ -64,6 +67,7 @@ def main(argv) -> None:
         seed = int(argv[argv.index("--perturb-ulp") + 1])
         up = np.random.default_rng(seed).integers(0, 2, Q.size).astype(bool)
         Q[:] = np.where(up, np.nextafter(Q, np.inf), np.nextafter(Q, -np.inf))
+    curve = []
     t0 = time.time()
     what = "one-ulp perturbed initial state" if perturb else "oracle with FMA contraction"
     print("%s, %s vs the fixture: step, est. rel L2, sample rel L2" % (name, what), flush=True)
@@ -71,12 +75,22 @@ def main(argv) -> None:
         while o.geti("iter") < it:
             o.step()
         err = LG.sketch_rel_l2(LG.sketch(Q), fx["sketch"][k], fx["norms"][k])
+        curve.append((float(it), err))
         line = "  %5d  %.3e" % (it, err)
         if k == len(fx["checkpoints"]) - 1:
             idx = fx["sample_idx"]
             line += "  %.3e" % (np.linalg.norm(Q[idx] - fx["sample"]) / np.linalg.norm(fx["sample"]))
         print(line + "   (%.0f s)" % (time.time() - t0), flush=True)
     o.close()
+    if "--record" in argv:
+        path = os.path.join(HERE, name + "_sensitivity.npz")
+        rec = {}
+        if os.path.exists(path):
+            with np.load(path) as z:
+                rec = {k: z[k] for k in z.files}
+        key = "ulp%d" % int(argv[argv.index("--perturb-ulp") + 1]) if perturb else "contracted"
+        rec[key] = np.array(curve)
+        np.savez_compressed(path, **rec)
 
 
 if __name__ == "__main__":

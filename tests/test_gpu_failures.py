@@ -47,3 +47,15 @@ def test_serving_reports_unreadable_requests_and_serves_the_rest(case_root, tmp_
     for mode in ("batched", "sequential"):
         res, _ = serve.serve(reqs, mode=mode)
         assert [r["status"] for r in res] == [0, CHORUS_EIO, 0], mode
+
+
+def test_serving_a_failing_solve_does_not_fail_the_next_one_in_its_slot(case_root):
+    """A request whose solve goes non-finite (an unstable time step) is reported as
+    CHORUS_ESTATE; the request admitted into the batch slot it leaves completes."""
+    bad = make_case(case_root, problem="orszag_tang", nx=8, ny=8, N=3, dt=0.5)  # far above the CFL limit
+    good = make_case(case_root, problem="orszag_tang", nx=8, ny=8, N=3, jitter=0.1, seed=6)
+    reqs = [(bad, 0.0, 100.0), (good, 0.0, 0.05), (good, 0.0, 0.03)]
+    res, _ = serve.serve(reqs, mode="batched", max_active=1)  # one solve at a time: the slot is reused
+    assert [r["status"] for r in res] == [CHORUS_ESTATE, 0, 0]
+    alone, _ = serve.serve(reqs[1:], mode="sequential")
+    assert [r["status"] for r in alone] == [0, 0]
