@@ -1,7 +1,6 @@
 """Committed golden fixtures (tests/golden/*.npz, made by tests/golden/make_golden.py
 from the oracle): the oracle must keep reproducing them (CPU), the product setup must
 reproduce their map digests (CPU), and the CUDA path must match them (GPU)."""
-import glob
 import hashlib
 import json
 import os
@@ -13,7 +12,18 @@ import oracle
 from chorus_mhd import Mesh, Solver, meshgen
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+
+
+def _short_cases():
+    """The fixtures make_golden.py writes (the long-horizon ones have their own tests)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(HERE, "golden", "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return list(mod.CASES)
+
+
+FIXTURES = sorted(os.path.join(HERE, "golden", n + ".npz") for n in _short_cases())
 MAPS = ["IF2C", "IC2F", "IF2V", "IBFINTER", "IBFREE", "CYC2FPAIR"]
 
 
@@ -46,7 +56,7 @@ def _check_state(Q, g, prefix, rtol):
 
 
 def test_fixtures_present():
-    assert len(FIXTURES) >= 7
+    assert len(FIXTURES) >= 7 and all(os.path.exists(p) for p in FIXTURES)
 
 
 @pytest.mark.parametrize("path", FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
