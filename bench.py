@@ -703,9 +703,10 @@ def run_reference(args):
 def main():
     global NX, N_SOL, JITTER, SEED, PROBLEM, MU, ETA0, WORKLOAD
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="C2", choices=sorted(WORKLOADS) + ["C5"],
+    ap.add_argument("--workload", default="C2", choices=sorted(WORKLOADS) + ["C4", "C5"],
                     help="C2: Orszag-Tang 512^2 jittered N=5 (default); C1: Orszag-Tang 64^2 N=4; "
-                         "C3: rotor 256^2 jittered N=4, FREE boundaries; C5: the serving stream on its "
+                         "C3: rotor 256^2 jittered N=4, FREE boundaries; C4: the ensemble leg alone "
+                         "(--ensemble-count solves, its own JSON line); C5: the serving stream on its "
                          "stated mix (its own JSON line)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
@@ -731,6 +732,12 @@ def main():
     args = ap.parse_args()
     if args.workload == "C5":
         run_serving_mix(args)
+        return
+    if args.workload == "C4":
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"metric": METRIC, "impl": "chorus",
+                          "ensemble": run_ensemble(args, 0, tempfile.mkdtemp(prefix="chorus_c4_"))}), flush=True)
         return
     MU, ETA0 = args.mu, args.eta0
     WORKLOAD = args.workload

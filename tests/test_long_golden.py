@@ -29,6 +29,22 @@ def test_every_long_fixture_is_present_and_consistent():
         assert np.all(np.abs(est / true - 1) < 0.15)
 
 
+def test_rotor_sensitivity_curves_are_recorded():
+    """The rotor's round-off spread that its long-run GPU test is held to: the oracle built
+    with FMA contraction and the oracle from a one-ulp perturbed start, each against the
+    fixture at every checkpoint, growing with the steps."""
+    name = "rotor_256x256_N4_500steps"
+    with np.load(os.path.join(HERE, "golden", name + "_sensitivity.npz")) as z:
+        cps = list(LG.load(name)["checkpoints"])
+        for key in ("contracted", "ulp1"):
+            c = z[key]
+            assert list(c[:, 0].astype(int)) == cps
+            assert np.all(np.isfinite(c[:, 1])) and c[-1, 1] > 100 * c[1, 1]
+        # a build of the same restatement that differs only in contraction ends further from
+        # the fixture than the 1e-10 bar
+        assert z["contracted"][-1, 1] > 1e-10
+
+
 def test_oracle_reproduces_first_checkpoint_of_orszag_tang_64():
     name = "ot_64x64_N4_1000steps"
     fx = LG.load(name)
