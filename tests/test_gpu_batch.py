@@ -17,6 +17,8 @@ MIX = [
     dict(problem="orszag_tang", nx=5, ny=6, N=2),
     dict(problem="orszag_tang", nx=4, ny=4, N=8, jitter=0.05, seed=5),
     dict(problem="orszag_tang", nx=6, ny=5, N=4, jitter=0.1, seed=6, mu=0.01, eta0=0.02),
+    dict(problem="orszag_tang", nx=1, ny=1, N=4),
+    dict(problem="alfven", nx=2, ny=1, N=3),
 ]
 
 

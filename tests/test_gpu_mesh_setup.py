@@ -25,6 +25,9 @@ MESHES = [
     dict(problem="alfven", nx=6, ny=5, N=5),
     dict(problem="orszag_tang", nx=33, ny=31, N=8, jitter=0.15, seed=4),
     dict(problem="rotor", nx=160, ny=150, N=4, jitter=0.1, seed=5),
+    dict(problem="orszag_tang", nx=1, ny=1, N=4),
+    dict(problem="alfven", nx=2, ny=1, N=3),
+    dict(problem="rotor", nx=1, ny=1, N=2),
 ]
 
 
