@@ -138,3 +138,28 @@ def test_sequential_mode_runs_fifo(case_root):
     res, mk = serve.serve(reqs, mode="sequential")
     assert all(r["status"] == 0 for r in res)
     assert res[1]["admit_s"] >= res[0]["finish_s"] - 1e-6
+
+
+def test_device_setup_serves_the_same_results(case_root):
+    """Requests set up on the device (gpu_setup) end in the same states as with the host
+    setup: the maps and geometry are the same bit for bit."""
+    specs = [dict(problem="orszag_tang", nx=10, ny=10, N=4, jitter=0.1, seed=1),
+             dict(problem="rotor", nx=64, ny=64, N=3, jitter=0.1, seed=5)]
+    dirs = [make_case(case_root, **sp) for sp in specs]
+    out = {}
+    for gpu_setup in (False, True):
+        qs = []
+        reqs = []
+        for k, d in enumerate(dirs):
+            m = Mesh(d)
+            q = np.empty(9 * m.N * m.N * m.ncell)
+            m.close()
+            qs.append(q)
+            # the rotor at this coarse grid goes non-finite after a few tens of steps (the
+            # reference's scheme does): about ten steps of it
+            reqs.append((d, 0.001 * k, 0.01 if k == 0 else 0.0015, {"Q": q}))
+        res, _ = serve.serve(reqs, mode="batched", gpu_setup=gpu_setup)
+        assert all(r["status"] == 0 for r in res)
+        out[gpu_setup] = qs
+    for a, b in zip(out[False], out[True]):
+        assert np.array_equal(a, b)
