@@ -256,7 +256,8 @@ def measure_e2e(sol, snap, it0, t0, steps: int, warmup: int, world: int):
     """The window again through the C-ABI with a host-resident state: every step uploads
     Q from pinned host memory, runs one step and downloads Q (chorus_gpu_step_host)."""
     import torch
-    qh = torch.empty(sol.nq, dtype=torch.float64, pin_memory=True).numpy()
+    qt = torch.empty(sol.nq, dtype=torch.float64, pin_memory=True)
+    qh = qt.numpy()
     qh[:] = snap
     for _ in range(max(1, min(warmup, 3))):  # untimed: first use of the copy stream and events
         sol.step_host(qh, qh, 1)
@@ -269,8 +270,28 @@ def measure_e2e(sol, snap, it0, t0, steps: int, warmup: int, world: int):
     t_1 = time.perf_counter()
     e2e_s = max_over_ranks(world, t_1 - t_0)
     dof = sol.ncell * sol.N * sol.N
+    link = link_rates(qt)
     return {"value": world * dof * 5 * steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 8 * sol.nq,
-            "d2h_bytes_per_step": 8 * sol.nq, "steps": steps}
+            "d2h_bytes_per_step": 8 * sol.nq, "steps": steps, "ms_per_step": e2e_s / steps * 1e3,
+            "link_gbs": link, "copy_ms_per_step": 8 * sol.nq / 1e6 * (1 / link["h2d"] + 1 / link["d2h"])}
+
+
+def link_rates(h) -> dict:
+    """Host link rates of this process (GB/s): one copy of the state each way between the
+    pinned host tensor h and a device buffer, CUDA events around each, best of two."""
+    import torch
+    g = torch.empty(h.numel(), dtype=torch.float64, device="cuda")
+    best = {"h2d": 0.0, "d2h": 0.0}
+    for _ in range(2):
+        for k, (dst, src) in (("h2d", (g, h)), ("d2h", (h, g))):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            dst.copy_(src, non_blocking=True)
+            b.record()
+            b.synchronize()
+            best[k] = max(best[k], 8 * h.numel() / (a.elapsed_time(b) * 1e6))
+    del g
+    return best
 
 
 def run_other_workloads(args, local, tmp, world):

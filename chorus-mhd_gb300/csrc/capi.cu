@@ -114,10 +114,10 @@ static int ensure_ops(int dev, int N, const double* Lmat, const double* Mmat, co
 struct Dispatch {
   void (*e1)(const SolveDev&, const Launch&, cudaStream_t, int, int, int);
   void (*e1ns)(const SolveDev&, const Launch&, cudaStream_t);
-  void (*f1)(const SolveDev&, cudaStream_t);
+  void (*f1)(const SolveDev&, cudaStream_t, int, int, int, int);
   void (*e2)(const SolveDev&, const Launch&, cudaStream_t);
   void (*f2)(const SolveDev&, cudaStream_t);
-  void (*e3)(const SolveDev&, const RKStage&, const Launch&, cudaStream_t);
+  void (*e3)(const SolveDev&, const RKStage&, const Launch&, cudaStream_t, int, int);
   void (*ct)(const SolveDev&, const Launch&, cudaStream_t, int, int, int);
   void (*nqsp)(const SolveDev&, int, int, cudaStream_t);
   void (*divb)(const SolveDev&, cudaStream_t);
@@ -152,7 +152,24 @@ using namespace chorus;
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
-constexpr int kHostChunks = 8;  // chunks of a host-state upload / download
+constexpr int kMaxHostChunks = 32;  // chunks of a host-state upload / download
+
+constexpr int kMaxHostSegs = 2 * kMaxHostChunks + 2;
+
+// The chunks of a host-state step: cells [cut[k], cut[k+1]); two-sided faces [f2[k], f2[k+1])
+// (those whose larger cell is in chunk k) and FREE faces [f1[k], f1[k+1]) (cell in chunk
+// k).  The download goes by segments of cells [sb[i], se[i]) whose cells and face
+// neighbours all lie in chunks 0..sk[i]: the maximal runs of cells that complete with the
+// same chunk (with a structured numbering about one per chunk, shifted by a row), or the
+// chunks themselves when the runs are more than kMaxHostSegs.
+struct HostChunks {
+  int K = 0;
+  int cut[kMaxHostChunks + 1];
+  int f2[kMaxHostChunks + 1];
+  int f1[kMaxHostChunks + 1];
+  int nseg = 0;
+  int sb[kMaxHostSegs], se[kMaxHostSegs], sk[kMaxHostSegs];
+};
 
 struct ChorusCtx {
   int device = 0;
@@ -181,7 +198,12 @@ struct ChorusCtx {
   std::vector<double> Lmat, Mmat, Xs, Xf;
   // host-state steps: a copy stream and events that chain chunked copies to kernels
   cudaStream_t cp = nullptr;
-  cudaEvent_t ev[2 * kHostChunks + 1] = {};
+  cudaEvent_t ev[kMaxHostChunks + kMaxHostSegs + 1] = {};
+  int host_chunks = 8;  // option "host_chunks"
+  // the larger cell of each two-sided face and the cell of each FREE face, in list order
+  // (ascending), and per cell the largest index among itself and its face neighbours
+  std::vector<int> f2max, f1cell, cellrel;
+  HostChunks hc;  // built on first use for host_chunks (hc.K == 0: not built)
 };
 
 namespace chorus {
@@ -331,8 +353,21 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
     if (!cell_ok(cl) || !lf_ok(ll)) return fail(set_err(CHORUS_EMESH, "IF2C row %d inconsistent", f + 1));
     f1.push_back(make_int2(cl - 1, ll));
   }
+  // two-sided faces in the order of their larger cell, FREE faces in cell order, so that
+  // the faces whose cells all lie below a cell bound are a prefix of each list (a
+  // host-state step runs the face passes chunk by chunk behind its copies); every face
+  // pass writes per-cell slots and the wave speed is a maximum, so no result depends on
+  // the order
+  std::stable_sort(f2.begin(), f2.end(),
+                   [](const int4& a, const int4& b) { return std::max(a.x, a.z) < std::max(b.x, b.z); });
+  std::stable_sort(f1.begin(), f1.end(), [](const int2& a, const int2& b) { return a.x < b.x; });
   c->nface2 = (int)f2.size();
   c->nface1 = (int)f1.size();
+  c->f2max.resize(f2.size());
+  for (size_t i = 0; i < f2.size(); i++) c->f2max[i] = std::max(f2[i].x, f2[i].z);
+  c->f1cell.resize(f1.size());
+  for (size_t i = 0; i < f1.size(); i++) c->f1cell[i] = f1[i].x;
+  c->hc.K = 0;
   // face neighbours per cell (local face 1..4 -> cell across it, -1 at FREE faces)
   std::vector<int4> nbr(NC, make_int4(-1, -1, -1, -1)), nbrlf(NC, make_int4(0, 0, 0, 0));
   auto setn = [&](int cell, int lf, int other, int olf) {
@@ -342,6 +377,11 @@ int chorus_gpu_bind(const ChorusDims* dims, const int32_t* IF2C, const int32_t* 
   for (const int4& f : f2) {
     setn(f.x, f.y, f.z, f.w);
     setn(f.z, f.w, f.x, f.y);
+  }
+  c->cellrel.resize(NC);
+  for (int ic = 0; ic < NC; ic++) {
+    const int4 b = nbr[ic];
+    c->cellrel[ic] = std::max(std::max(ic, b.x), std::max(b.y, std::max(b.z, b.w)));
   }
 
   // ---- derived geometry
@@ -548,6 +588,12 @@ int chorus_gpu_set_option(ChorusCtx* c, const char* name, int64_t value) {
     c->plot_sensor = value ? 1 : 0;
     CK(cudaMemsetAsync((void*)c->sd.plot_flag, c->plot_sensor, sizeof(int), c->st));
     return CHORUS_OK;  // read by the kernels at run time: the graphs stay valid
+  } else if (n == "host_chunks") {
+    if (value < 1 || value > kMaxHostChunks)
+      return set_err(CHORUS_EINVAL, "host_chunks=%lld outside 1..%d", (long long)value, kMaxHostChunks);
+    c->host_chunks = (int)value;
+    c->hc.K = 0;
+    return CHORUS_OK;  // the step graphs do not use it
   } else if (n == "skip_inactive_viscous") {
     c->skip_option = value ? 1 : 0;
     c->sd.skip = (c->skip_option && c->p.mu == 0.0 && c->p.eta0 == 0.0) ? 1 : 0;
@@ -581,6 +627,7 @@ int64_t chorus_gpu_get_option(ChorusCtx* c, const char* name) {
   if (n == "skip_inactive_viscous") return c->skip_option;
   if (n == "diagnostics") return c->diagnostics;
   if (n == "plot_sensor") return c->plot_sensor;
+  if (n == "host_chunks") return c->host_chunks;
   if (n == "skip_active") return c->sd.skip;
   const char* pass[4] = {"e1", "e2", "e3", "ct"};
   for (int i = 0; i < 4; i++) {
@@ -622,9 +669,9 @@ void enqueue_stage(ChorusCtx* c, const RKStage& rk, bool last) {
   const SolveDev& s = c->sd;
   c->D->e1(s, c->L[0], c->st, last ? 1 : 0, 0, -1);  // also zeroes the stage's wave speed
   c->qvf9_pending = false;
-  c->D->f1(s, c->st);
+  c->D->f1(s, c->st, 0, -1, 0, -1);
   c->D->e2(s, c->L[1], c->st);  // also the face AV viscosities
-  c->D->e3(s, rk, c->L[2], c->st);  // averages the grad Q traces where it reads them
+  c->D->e3(s, rk, c->L[2], c->st, 0, -1);  // averages the grad Q traces where it reads them
 }
 
 void enqueue_ct(ChorusCtx* c) {
@@ -709,48 +756,107 @@ void enqueue_diag(ChorusCtx* c) {
   k_store_record<<<1, 1, 0, c->st>>>(c->red, c->sd.eig, c->red + 4);
 }
 
-// One step whose state comes from / goes to host memory: the upload of Q runs on the
-// copy stream in chunks of cells, each chunk's E1 of the first stage starting as soon as
-// its cells have arrived; the download follows the last CT pass chunk by chunk.  E1 and
-// that CT pass are cell-local, so the chunks are independent.
+const HostChunks& host_chunks(ChorusCtx* c) {
+  HostChunks& h = c->hc;
+  if (h.K) return h;
+  const int NC = c->sd.NC;
+  h.K = std::max(1, std::min(c->host_chunks, NC / 1024));
+  for (int k = 0; k <= h.K; k++) {
+    h.cut[k] = (int)((long long)NC * k / h.K);
+    h.f2[k] = (int)(std::lower_bound(c->f2max.begin(), c->f2max.end(), h.cut[k]) - c->f2max.begin());
+    h.f1[k] = (int)(std::lower_bound(c->f1cell.begin(), c->f1cell.end(), h.cut[k]) - c->f1cell.begin());
+  }
+  // the chunk that completes each cell's neighbourhood (cellrel >= the cell itself)
+  auto chunk_of = [&](int ic) {
+    return (int)(std::upper_bound(h.cut + 1, h.cut + h.K + 1, ic) - (h.cut + 1));
+  };
+  h.nseg = 0;
+  for (int ic = 0; ic < NC;) {
+    const int k = chunk_of(c->cellrel[ic]);
+    int e = ic + 1;
+    while (e < NC && chunk_of(c->cellrel[e]) == k) e++;
+    if (h.nseg == kMaxHostSegs) {
+      h.nseg = -1;
+      break;
+    }
+    h.sb[h.nseg] = ic;
+    h.se[h.nseg] = e;
+    h.sk[h.nseg] = k;
+    h.nseg++;
+    ic = e;
+  }
+  if (h.nseg < 0) {  // fragmented: whole chunks, each when its last neighbour is through
+    h.nseg = h.K;
+    for (int j = 0; j < h.K; j++) {
+      int r = h.cut[j + 1] - 1;
+      for (int ic = h.cut[j]; ic < h.cut[j + 1]; ic++) r = std::max(r, c->cellrel[ic]);
+      h.sb[j] = h.cut[j];
+      h.se[j] = h.cut[j + 1];
+      h.sk[j] = chunk_of(r);
+    }
+  }
+  return h;
+}
+
+// One step whose state comes from / goes to host memory, the copies (on the copy stream,
+// in chunks of cells) overlapped with the passes that can run chunk by chunk:
+//  - the first stage's E1 on each chunk as soon as its cells have arrived, and F1 on the
+//    faces whose cells have all been through E1 (E2 waits for every face: it reads the
+//    stage's maximum wave speed);
+//  - the last stage's E3 chunk by chunk, each chunk followed by the A_z traces of the CT
+//    projection and their average on the faces whose cells are all updated; a run of
+//    cells whose cells and face neighbours are all through that gets its B (the last CT
+//    pass) and its download.
+// Every pass runs on every cell and face exactly once, as in the step graph, so the
+// results are the graph's bit for bit.
 void enqueue_step_host(ChorusCtx* c, bool diag, const double* Qin, double* Qout) {
   const SolveDev& s = c->sd;
-  const int NC = s.NC;
+  const HostChunks& h = host_chunks(c);
+  const int K = h.K;
   const size_t per = (size_t)s.N * s.N * 9;
-  const int K = std::max(1, std::min(kHostChunks, NC / 1024));
-  auto cut = [&](int i) { return (int)((long long)NC * i / K); };
+  auto off = [&](int j) { return (size_t)h.cut[j] * per; };
+  auto bytes = [&](int j) { return (size_t)(h.cut[j + 1] - h.cut[j]) * per * sizeof(double); };
+  auto off_s = [&](int i) { return (size_t)h.sb[i] * per; };
+  auto bytes_s = [&](int i) { return (size_t)(h.se[i] - h.sb[i]) * per * sizeof(double); };
   RKStage r[5];
   make_rk(c, diag, r);
   if (Qin) {
-    cudaEventRecord(c->ev[2 * kHostChunks], c->st);  // earlier work on the state is done
-    cudaStreamWaitEvent(c->cp, c->ev[2 * kHostChunks], 0);
-    for (int i = 0; i < K; i++) {
-      const int a = cut(i), b = cut(i + 1);
-      cudaMemcpyAsync(s.Q + a * per, Qin + a * per, (size_t)(b - a) * per * sizeof(double), cudaMemcpyHostToDevice,
-                      c->cp);
-      cudaEventRecord(c->ev[i], c->cp);
-      cudaStreamWaitEvent(c->st, c->ev[i], 0);
-      c->D->e1(s, c->L[0], c->st, 0, a, b);
+    cudaEventRecord(c->ev[kMaxHostChunks + kMaxHostSegs], c->st);  // earlier work on the state is done
+    cudaStreamWaitEvent(c->cp, c->ev[kMaxHostChunks + kMaxHostSegs], 0);
+    for (int k = 0; k < K; k++) {
+      cudaMemcpyAsync(s.Q + off(k), Qin + off(k), bytes(k), cudaMemcpyHostToDevice, c->cp);
+      cudaEventRecord(c->ev[k], c->cp);
+      cudaStreamWaitEvent(c->st, c->ev[k], 0);
+      c->D->e1(s, c->L[0], c->st, 0, h.cut[k], h.cut[k + 1]);  // the first chunk zeroes the wave speed
+      c->D->f1(s, c->st, h.f2[k], h.f2[k + 1], h.f1[k], h.f1[k + 1]);
     }
   } else {
     c->D->e1(s, c->L[0], c->st, 0, 0, -1);
+    c->D->f1(s, c->st, 0, -1, 0, -1);
   }
-  c->D->f1(s, c->st);
   c->D->e2(s, c->L[1], c->st);
-  c->D->e3(s, r[0], c->L[2], c->st);
-  for (int k = 1; k < 5; k++) enqueue_stage(c, r[k], k == 4);
-  c->D->ct(s, c->L[3], c->st, 0, 0, -1);
-  c->D->ct(s, c->L[3], c->st, 1, 0, -1);
+  c->D->e3(s, r[0], c->L[2], c->st, 0, -1);
+  for (int k = 1; k < 4; k++) enqueue_stage(c, r[k], false);
+  c->D->e1(s, c->L[0], c->st, 1, 0, -1);
+  c->D->f1(s, c->st, 0, -1, 0, -1);
+  c->D->e2(s, c->L[1], c->st);
   if (Qout) {
-    for (int i = 0; i < K; i++) {
-      const int a = cut(i), b = cut(i + 1);
-      c->D->ct(s, c->L[3], c->st, 2, a, b);
-      cudaEventRecord(c->ev[kHostChunks + i], c->st);
-      cudaStreamWaitEvent(c->cp, c->ev[kHostChunks + i], 0);
-      cudaMemcpyAsync(Qout + a * per, s.Q + a * per, (size_t)(b - a) * per * sizeof(double), cudaMemcpyDeviceToHost,
-                      c->cp);
+    for (int k = 0; k < K; k++) {
+      c->D->e3(s, r[4], c->L[2], c->st, h.cut[k], h.cut[k + 1]);
+      c->D->ct(s, c->L[3], c->st, 0, h.cut[k], h.cut[k + 1]);
+      c->D->ct(s, c->L[3], c->st, 1, h.f2[k], h.f2[k + 1]);
+      for (int i = 0; i < h.nseg; i++) {
+        if (h.sk[i] != k) continue;
+        c->D->ct(s, c->L[3], c->st, 2, h.sb[i], h.se[i]);
+        cudaEventRecord(c->ev[kMaxHostChunks + i], c->st);
+        cudaStreamWaitEvent(c->cp, c->ev[kMaxHostChunks + i], 0);
+        cudaMemcpyAsync(Qout + off_s(i), s.Q + off_s(i), bytes_s(i), cudaMemcpyDeviceToHost, c->cp);
+      }
     }
   } else {
+    c->D->e3(s, r[4], c->L[2], c->st, 0, -1);
+    c->D->ct(s, c->L[3], c->st, 0, 0, -1);
+    c->D->ct(s, c->L[3], c->st, 1, 0, -1);
     c->D->ct(s, c->L[3], c->st, 2, 0, -1);
   }
   c->qvf9_pending = true;
@@ -812,7 +918,7 @@ int comp_inviscid_flux_gpu(ChorusCtx* c) {
   if (ctx_device(c)) return CHORUS_ECUDA;
   c->D->e1ns(c->sd, c->L[0], c->st);
   c->qvf9_pending = false;
-  c->D->f1(c->sd, c->st);
+  c->D->f1(c->sd, c->st, 0, -1, 0, -1);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
   return CHORUS_OK;
@@ -972,12 +1078,12 @@ int chorus_gpu_profile_stage(ChorusCtx* c, int32_t reps, double* ms) {
     c->D->e1(s, c->L[0], c->st, 0, 0, -1);
     c->qvf9_pending = false;
     CK(cudaEventRecord(ev[1], c->st));
-    c->D->f1(s, c->st);
+    c->D->f1(s, c->st, 0, -1, 0, -1);
     CK(cudaEventRecord(ev[2], c->st));
     c->D->e2(s, c->L[1], c->st);
     CK(cudaEventRecord(ev[3], c->st));
     CK(cudaEventRecord(ev[4], c->st));  // the former F2 pass lives in E2 and E3
-    c->D->e3(s, r, c->L[2], c->st);
+    c->D->e3(s, r, c->L[2], c->st, 0, -1);
     CK(cudaEventRecord(ev[5], c->st));
     CK(cudaEventSynchronize(ev[5]));
     float t;

@@ -143,10 +143,13 @@ struct Launch {
 // plot != 0: also record the variable-6 sensor (Se6) when AV is on
 // cells [c0, c1) (c1 < 0: to the end)
 template <int N> void launch_e1(const SolveDev& s, const Launch& L, cudaStream_t st, int plot, int c0 = 0, int c1 = -1);
-template <int N> void launch_f1(const SolveDev& s, cudaStream_t st);
+// two-sided faces [a2, b2) and FREE faces [a1, b1) (b < 0: to the end of the list)
+template <int N> void launch_f1(const SolveDev& s, cudaStream_t st, int a2 = 0, int b2 = -1, int a1 = 0, int b1 = -1);
 template <int N> void launch_e2(const SolveDev& s, const Launch& L, cudaStream_t st);
 template <int N> void launch_f2(const SolveDev& s, cudaStream_t st);
-template <int N> void launch_e3(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st);
+template <int N> void launch_e3(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st, int c0 = 0,
+                                int c1 = -1);
+// modes 0 and 2: cells [c0, c1); mode 1 (the face average): two-sided faces [c0, c1)
 template <int N> void launch_ct(const SolveDev& s, const Launch& L, cudaStream_t st, int mode, int c0 = 0, int c1 = -1);
 // the diagnostic's B_x, B_y traces: mode 0 interpolation, mode 1 face average
 template <int N> void launch_diag(const SolveDev& s, const Launch& L, cudaStream_t st, int mode);

@@ -511,10 +511,14 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
   return evb;
 }
 
+// face points [t2, t2 + n2) of the two-sided list, then [t1, t1 + n - n2) of the FREE list
+// (f1_point numbering: the FREE faces follow the two-sided ones)
 template <int N>
-__global__ void __launch_bounds__(256) k_f1(SolveDev s) {
+__global__ void __launch_bounds__(256) k_f1(SolveDev s, int t2, int n2, int t1, int n) {
   pdl_wait();
-  const unsigned long long evb = f1_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long evb = 0ull;
+  if (i < n) evb = f1_point<N>(s, i < n2 ? t2 + i : t1 + (i - n2));
   block_max_ull(evb, s.eig);
 }
 
@@ -861,11 +865,11 @@ __device__ __forceinline__ void e3_body(const SolveDev& s, int e0, int cnt, int 
 }
 
 template <int N>
-__global__ void __launch_bounds__(512) k_e3(SolveDev s, RKStage rk, int epb, int update) {
+__global__ void __launch_bounds__(512) k_e3(SolveDev s, RKStage rk, int epb, int update, int c0, int c1) {
   extern __shared__ __align__(16) double sm[];
   pdl_wait();
-  const int e0 = blockIdx.x * epb;
-  const int cnt = min(epb, s.NC - e0);
+  const int e0 = c0 + blockIdx.x * epb;
+  const int cnt = min(epb, c1 - e0);
   if (cnt <= 0) return;
   e3_body<N, OpsTU>(s, e0, cnt, epb, rk, update, sm);
 }
@@ -967,10 +971,12 @@ __device__ __forceinline__ void ctface_point(const SolveDev& s, int t) {
   s.Azf[gr] = v;
 }
 
+// the points of two-sided faces [f0, f1)
 template <int N>
-__global__ void __launch_bounds__(256) k_ct_face(SolveDev s) {
+__global__ void __launch_bounds__(256) k_ct_face(SolveDev s, int f0, int f1) {
   pdl_wait();
-  ctface_point<N>(s, blockIdx.x * blockDim.x + threadIdx.x);
+  const int t = f0 * N + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < f1 * N) ctface_point<N>(s, t);
 }
 
 // The diagnostic of iterations.f90:35-36 (comp_inviscid_flux, then nablaQsp(6,7) for

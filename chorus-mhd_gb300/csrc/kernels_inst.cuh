@@ -59,9 +59,13 @@ void CHORUS_CAT(launch_e1_nosensor_n, CHORUS_N)(const SolveDev& s, const Launch&
   launch_pdl(k_e1<kN>, grid_cells(s.NC, L.epb), L.threads, smem_e1(L.epb), st, s, L.epb, 0, 0, s.NC);
 }
 template <>
-void launch_f1<kN>(const SolveDev& s, cudaStream_t st) {
-  const int n = (s.nface2 + s.nface1) * kN;
-  if (n > 0) launch_pdl(k_f1<kN>, (n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st, s);
+void launch_f1<kN>(const SolveDev& s, cudaStream_t st, int a2, int b2, int a1, int b1) {
+  if (b2 < 0) b2 = s.nface2;
+  if (b1 < 0) b1 = s.nface1;
+  const int n2 = (b2 - a2) * kN, n = n2 + (b1 - a1) * kN;
+  if (n > 0)
+    launch_pdl(k_f1<kN>, (n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st, s, a2 * kN, n2,
+               (s.nface2 + a1) * kN, n);
 }
 template <>
 void launch_e2<kN>(const SolveDev& s, const Launch& L, cudaStream_t st) {
@@ -87,15 +91,19 @@ void launch_f2<kN>(const SolveDev& s, cudaStream_t st) {
   if (n > 0) k_f2<kN><<<(n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st>>>(s);
 }
 template <>
-void launch_e3<kN>(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st) {
+void launch_e3<kN>(const SolveDev& s, const RKStage& rk, const Launch& L, cudaStream_t st, int c0, int c1) {
   const int update = (rk.cQ != 0.0 || rk.cR != 0.0 || rk.nsrc > 0) ? 1 : 0;
-  launch_pdl(k_e3<kN>, grid_cells(s.NC, L.epb), L.threads, smem_e3(L.epb), st, s, rk, L.epb, update);
+  if (c1 < 0) c1 = s.NC;
+  if (c1 > c0)
+    launch_pdl(k_e3<kN>, grid_cells(c1 - c0, L.epb), L.threads, smem_e3(L.epb), st, s, rk, L.epb, update, c0, c1);
 }
 template <>
 void launch_ct<kN>(const SolveDev& s, const Launch& L, cudaStream_t st, int mode, int c0, int c1) {
   if (mode == 1) {
-    const int n = s.nface2 * kN;
-    if (n > 0) launch_pdl(k_ct_face<kN>, (n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st, s);
+    if (c1 < 0) c1 = s.nface2;
+    const int n = (c1 - c0) * kN;
+    if (n > 0)
+      launch_pdl(k_ct_face<kN>, (n + face_threads(n) - 1) / face_threads(n), face_threads(n), 0, st, s, c0, c1);
   } else {
     if (c1 < 0) c1 = s.NC;
     if (c1 > c0)

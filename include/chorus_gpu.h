@@ -143,12 +143,15 @@ int iterations_gpu(ChorusCtx* ctx, int32_t nsteps, int32_t* iter, double* ctime,
                    int32_t max_diag, int32_t* n_diag);
 /* iterations_gpu on a state that lives in host memory, as the reference's own Q does
  * (setup2d.f90:54): Q(9,N,N,NCELL) is read from Qin before the first step and written to
- * Qout after the last one (either may be NULL; they may be the same buffer).  The upload
- * runs in chunks of cells on a second stream, each chunk's first residual pass starting
- * as soon as its cells have arrived, and the download follows the CT projection chunk by
- * chunk, so the copies overlap the kernels; with pinned host memory the overlap is full,
- * pageable memory is accepted and copied synchronously.  No counterpart in the
- * reference (its Q never leaves the host). */
+ * Qout after the last one (either may be NULL; they may be the same buffer).  A state of
+ * 64 MB or more is copied in chunks of cells on a second stream (option "host_chunks"):
+ * the first stage's interior and face flux passes run on each chunk as soon as its cells
+ * (and their face neighbours) have arrived, and the last stage's update and the CT
+ * projection run chunk by chunk, each chunk's download starting once its cells and their
+ * face neighbours are final.  With pinned host memory the copies overlap the kernels;
+ * pageable memory is accepted and copied synchronously.  The results are those of
+ * iterations_gpu bit for bit.  No counterpart in the reference (its Q never leaves the
+ * host). */
 int chorus_gpu_step_host(ChorusCtx* ctx, const double* Qin, double* Qout, int32_t nsteps, int32_t* iter,
                          double* ctime, ChorusDiag* diag, int32_t max_diag, int32_t* n_diag);
 
@@ -225,6 +228,9 @@ int chorus_gpu_profile_stage(ChorusCtx* ctx, int32_t reps, double* ms);
  *   "plot_sensor" (default 0): the last stage of each step also records the AV sensor
  *       of variable 6, which only the plot output reads (about 1% of a step); takes
  *       effect on the stream in order, without rebuilding the step graphs;
+ *   "host_chunks" (1..32, default 8): chunks of cells in which chorus_gpu_step_host
+ *       copies a state of 64 MB or more, each chunk's copy overlapped with the passes
+ *       that can run on it (fewer for meshes under 1024 cells per chunk);
  *   "epb_e1" / "epb_e2" / "epb_e3" / "epb_ct" (1..64): cells per CTA of a cell pass;
  *   "threads_e1" / "threads_e2" / "threads_e3" (32..512) and "threads_ct" (32..256), multiples of 32:
  *       threads per CTA.

@@ -346,17 +346,34 @@ def test_skipping_inactive_viscous_work_changes_nothing(case_root, case):
     assert np.array_equal(res[0], res[1])
 
 
-@pytest.mark.parametrize("nx,ny,nsteps", [(72, 64, 1), (72, 64, 3), (256, 240, 1), (256, 240, 12)])
-def test_step_host_equals_resident_steps(case_root, nx, ny, nsteps):
+def test_host_chunks_option_range(case_root):
+    d = make_case(case_root, problem="orszag_tang", nx=8, ny=8, N=3)
+    s = Solver(Mesh(d))
+    assert s.get_option("host_chunks") == 8
+    for bad in (0, 33):
+        with pytest.raises(Exception, match="host_chunks"):
+            s.set_option("host_chunks", bad)
+    assert s.get_option("host_chunks") == 8
+    s.close()
+
+
+@pytest.mark.parametrize("problem,nx,ny,nsteps,chunks", [
+    ("orszag_tang", 72, 64, 1, 16), ("orszag_tang", 72, 64, 3, 16), ("orszag_tang", 256, 240, 1, 16),
+    ("orszag_tang", 256, 240, 12, 16), ("orszag_tang", 256, 240, 2, 5), ("orszag_tang", 256, 240, 2, 32),
+    ("rotor", 256, 240, 2, 16), ("rotor", 256, 240, 1, 7)])
+def test_step_host_equals_resident_steps(case_root, problem, nx, ny, nsteps, chunks):
     """chorus_gpu_step_host gives the same bits as upload + iterations_gpu + download, for
     pageable and pinned host buffers: small states (plain copies around the step graph)
-    and states of 64 MB and more (chunked copies overlapping the cell-local passes)."""
-    d = make_case(case_root, problem="orszag_tang", nx=nx, ny=ny, N=4, jitter=0.1, seed=21)
+    and states of 64 MB and more (chunked copies overlapping the first stage's E1/F1 and
+    the last stage's E3 and CT passes), periodic and FREE boundaries, several chunk counts."""
+    d = make_case(case_root, problem=problem, nx=nx, ny=ny, N=4, jitter=0.1, seed=21)
     a = Solver(Mesh(d))
     Q0 = a.state()
     ref_diag = a.iterations(nsteps)
     ref = a.state()
     b = Solver(Mesh(d))
+    b.set_option("host_chunks", chunks)
+    assert b.get_option("host_chunks") == chunks
     out = np.empty_like(Q0)
     diag = b.step_host(Q0.copy(), out, nsteps)
     assert np.array_equal(out, ref)
@@ -367,6 +384,7 @@ def test_step_host_equals_resident_steps(case_root, nx, ny, nsteps):
     pin = torch.empty(Q0.size, dtype=torch.float64, pin_memory=True).numpy()
     pin[:] = Q0
     c = Solver(Mesh(d))
+    c.set_option("host_chunks", chunks)
     c.step_host(pin, pin, nsteps)
     assert np.array_equal(pin, ref)
     for s in (a, b, c):
