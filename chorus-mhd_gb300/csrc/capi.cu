@@ -171,6 +171,18 @@ struct HostChunks {
   int sb[kMaxHostSegs], se[kMaxHostSegs], sk[kMaxHostSegs];
 };
 
+// A host-state step captured as a CUDA graph for one pair of pinned host buffers (its
+// copies address them) and one kind of step (with or without the diagnostic), so that a
+// step is one launch however busy the host thread is
+struct HostGraph {
+  const double* qin = nullptr;
+  double* qout = nullptr;
+  int diag = 0;
+  cudaGraphExec_t ex = nullptr;
+};
+constexpr int kHostGraphs = 4;
+constexpr int kEvJoin = kMaxHostChunks + kMaxHostSegs + 1;  // the copy stream's join event
+
 struct ChorusCtx {
   int device = 0;
   ChorusDims dims{};
@@ -198,13 +210,22 @@ struct ChorusCtx {
   std::vector<double> Lmat, Mmat, Xs, Xf;
   // host-state steps: a copy stream and events that chain chunked copies to kernels
   cudaStream_t cp = nullptr;
-  cudaEvent_t ev[kMaxHostChunks + kMaxHostSegs + 1] = {};
+  cudaEvent_t ev[kMaxHostChunks + kMaxHostSegs + 2] = {};
   int host_chunks = 8;  // option "host_chunks"
   // the larger cell of each two-sided face and the cell of each FREE face, in list order
   // (ascending), and per cell the largest index among itself and its face neighbours
   std::vector<int> f2max, f1cell, cellrel;
   HostChunks hc;  // built on first use for host_chunks (hc.K == 0: not built)
+  HostGraph hg[kHostGraphs];
+  int hg_next = 0;
 };
+
+static void drop_host_graphs(ChorusCtx* c) {
+  for (HostGraph& g : c->hg) {
+    if (g.ex) cudaGraphExecDestroy(g.ex);
+    g = HostGraph{};
+  }
+}
 
 namespace chorus {
 void upload_ops_all(int N, const OpsN& o);
@@ -546,6 +567,7 @@ int chorus_gpu_free(ChorusCtx* c) {
   cudaSetDevice(c->device);
   if (c->g_step) cudaGraphExecDestroy(c->g_step);
   if (c->g_diag) cudaGraphExecDestroy(c->g_diag);
+  drop_host_graphs(c);
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->arena) cudaFree(c->arena);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
@@ -562,6 +584,7 @@ static void drop_graphs(ChorusCtx* c) {
   if (c->g_step) cudaGraphExecDestroy(c->g_step);
   if (c->g_diag) cudaGraphExecDestroy(c->g_diag);
   c->g_step = c->g_diag = nullptr;
+  drop_host_graphs(c);
 }
 
 int chorus_gpu_set_params(ChorusCtx* c, const ChorusParams* p) {
@@ -593,6 +616,7 @@ int chorus_gpu_set_option(ChorusCtx* c, const char* name, int64_t value) {
       return set_err(CHORUS_EINVAL, "host_chunks=%lld outside 1..%d", (long long)value, kMaxHostChunks);
     c->host_chunks = (int)value;
     c->hc.K = 0;
+    drop_host_graphs(c);
     return CHORUS_OK;  // the step graphs do not use it
   } else if (n == "skip_inactive_viscous") {
     c->skip_option = value ? 1 : 0;
@@ -863,6 +887,49 @@ void enqueue_step_host(ChorusCtx* c, bool diag, const double* Qin, double* Qout)
   if (diag) enqueue_diag(c);  // reads Q only: it may overlap the download
 }
 
+// page-locked host memory (cudaHostAlloc / cudaHostRegister), which a captured copy may
+// address; null counts as such (no copy)
+bool pinned_host(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// the captured host-state step for (qin, qout, diag), captured on first use; the copy
+// stream joins the main stream at its end, so the graph's completion covers the download
+cudaGraphExec_t host_graph(ChorusCtx* c, bool diag, const double* qin, double* qout) {
+  for (const HostGraph& g : c->hg)
+    if (g.ex && g.qin == qin && g.qout == qout && g.diag == (int)diag) return g.ex;
+  HostGraph& g = c->hg[c->hg_next];
+  c->hg_next = (c->hg_next + 1) % kHostGraphs;
+  if (g.ex) cudaGraphExecDestroy(g.ex);
+  g = HostGraph{};
+  if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
+  enqueue_step_host(c, diag, qin, qout);
+  cudaEventRecord(c->ev[kEvJoin], c->cp);
+  cudaStreamWaitEvent(c->st, c->ev[kEvJoin], 0);
+  cudaGraph_t gr = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->st, &gr);
+  if (e != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    return nullptr;
+  }
+  e = cudaGraphInstantiate(&g.ex, gr, 0);
+  cudaGraphDestroy(gr);
+  if (e != cudaSuccess) {
+    g.ex = nullptr;
+    return nullptr;
+  }
+  g.qin = qin;
+  g.qout = qout;
+  g.diag = diag ? 1 : 0;
+  return g.ex;
+}
+
 int build_graphs(ChorusCtx* c) {
   drop_graphs(c);
   for (int which = 0; which < 2; which++) {
@@ -1016,9 +1083,20 @@ static int run_steps(ChorusCtx* c, int32_t nsteps, int32_t* iter, double* ctime,
     double* qout = s == nsteps - 1 ? Qout : nullptr;
     const size_t qbytes = (size_t)c->dims.NCELL * N * N * 9 * sizeof(double);
     if ((qin || qout) && qbytes >= ((size_t)64 << 20)) {
-      // large states: copies in chunks, overlapped with the cell-local passes
-      enqueue_step_host(c, d, qin, qout);
-      CK(cudaGetLastError());
+      // large states: copies in chunks, overlapped with the passes that can run chunk by
+      // chunk; one graph launch for pinned buffers, the calls one by one for pageable
+      // ones (a copy from pageable memory cannot be captured)
+      if (pinned_host(qin) && pinned_host(qout)) {
+        cudaGraphExec_t ex = host_graph(c, d, qin, qout);
+        if (!ex) {
+          cudaGetLastError();
+          return set_err(CHORUS_ECUDA, "capturing the host-state step failed");
+        }
+        CK(cudaGraphLaunch(ex, c->st));
+      } else {
+        enqueue_step_host(c, d, qin, qout);
+        CK(cudaGetLastError());
+      }
     } else {
       // small states: the copies take less than the launches a chunked step would add
       if (qin) CK(cudaMemcpyAsync(c->sd.Q, qin, qbytes, cudaMemcpyHostToDevice, c->st));

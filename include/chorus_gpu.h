@@ -148,8 +148,9 @@ int iterations_gpu(ChorusCtx* ctx, int32_t nsteps, int32_t* iter, double* ctime,
  * the first stage's interior and face flux passes run on each chunk as soon as its cells
  * (and their face neighbours) have arrived, and the last stage's update and the CT
  * projection run chunk by chunk, each chunk's download starting once its cells and their
- * face neighbours are final.  With pinned host memory the copies overlap the kernels;
- * pageable memory is accepted and copied synchronously.  The results are those of
+ * face neighbours are final.  With pinned host memory the copies overlap the kernels and
+ * the step is captured as a CUDA graph on first use for each (Qin, Qout) pair and replayed
+ * after; pageable memory is accepted and copied synchronously.  The results are those of
  * iterations_gpu bit for bit.  No counterpart in the reference (its Q never leaves the
  * host). */
 int chorus_gpu_step_host(ChorusCtx* ctx, const double* Qin, double* Qout, int32_t nsteps, int32_t* iter,

@@ -346,6 +346,36 @@ def test_skipping_inactive_viscous_work_changes_nothing(case_root, case):
     assert np.array_equal(res[0], res[1])
 
 
+def test_step_host_graph_cache(case_root):
+    """The captured host-state steps (one graph per pinned buffer pair and step kind) give
+    the resident run's bits while the buffers alternate, a pageable buffer (the uncaptured
+    path) comes between them, the chunk count changes and the time step changes."""
+    torch = pytest.importorskip("torch")
+    d = make_case(case_root, problem="orszag_tang", nx=256, ny=240, N=4, jitter=0.1, seed=21)
+    a = Solver(Mesh(d))
+    b = Solver(Mesh(d))
+    q = a.state()
+    dt0 = a.mesh.params.dt
+    pins = [torch.empty(q.size, dtype=torch.float64, pin_memory=True).numpy() for _ in range(2)]
+    page = np.empty_like(q)
+    bufs = [pins[0], pins[1], page, pins[0], pins[1], pins[0], pins[1], pins[0], pins[1], pins[0], pins[1], pins[0]]
+    for k, buf in enumerate(bufs):
+        if k == 5:
+            for s in (a, b):
+                s.set_params(dt=0.5 * dt0)
+        if k == 8:
+            b.set_option("host_chunks", 3)
+        buf[:] = q
+        b.step_host(buf, buf, 1)
+        a.iterations(1)
+        q = a.state()
+        assert np.array_equal(buf, q), "step %d" % (k + 1)
+    assert b.iter == a.iter and b.ctime == a.ctime
+    assert [r["residglob"] for r in b.diagnostics] == [r["residglob"] for r in a.diagnostics]
+    a.close()
+    b.close()
+
+
 def test_host_chunks_option_range(case_root):
     d = make_case(case_root, problem="orszag_tang", nx=8, ny=8, N=3)
     s = Solver(Mesh(d))
