@@ -71,11 +71,16 @@ static void make_ops(int N, const double* Lmat, const double* Mmat, const double
     }
     o.LMID[f] = (N & 1) ? Lmat[f + (N + 1) * ((N - 1) / 2)] : 0.0;
   }
-  o.LS = fix_shift_for(Lmat, (N + 1) * N);
+  // the integer line operators in mirror form: Lmat as the row-major (N+1) x N operator
+  // L(f, j), Mmat (column-major (N+1, N)) is already the row-major N x (N+1) operator
+  // M(r, i) indexed [i][r]
+  double Lrow[(kMaxN + 1) * kMaxN];
   for (int f = 0; f <= N; f++)
-    for (int j = 0; j < N; j++) fix_split_coef(Lmat[f + (N + 1) * j], o.LS, &o.LH[f * N + j], &o.LL[f * N + j]);
+    for (int j = 0; j < N; j++) Lrow[f * N + j] = Lmat[f + (N + 1) * j];
+  o.LS = fix_shift_for(Lmat, (N + 1) * N);
+  fix_mirror_coefs(Lrow, N + 1, N, 1, o.LS, o.LH, o.LL);
   o.MS = fix_shift_for(Mmat, (N + 1) * N);
-  for (int i = 0; i < (N + 1) * N; i++) fix_split_coef(Mmat[i], o.MS, &o.MH[i], &o.ML[i]);
+  fix_mirror_coefs(Mmat, N, N + 1, -1, o.MS, o.MH, o.ML);
   // AV smoothing A = Hlow * H: project N points onto the N-1 low-order points
   // (hhval at Xs_low, AV.f90:19-35) and evaluate back (hhval_low at Xs, :41-58)
   double xsl[kMaxN], xfl[kMaxN + 1];

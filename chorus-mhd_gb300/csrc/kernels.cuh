@@ -74,12 +74,13 @@ struct OpsN {
   double CE[kHalfF * kHalfS];
   double CO[kHalfF * kHalfS];
   double LMID[kHalfF];
-  // the integer form of Lmat (fixdot.cuh): LH/LL[f*N + j] = limbs of round(L(f,j) 2^LS)
+  // the integer form of Lmat (fixdot.cuh) in mirror form (fix_mirror_coefs, sigma = +1,
+  // C(f, j) = L(f, j): rows f <= N/2 of N limbs) at scale 2^LS
   int LH[(kMaxN + 1) * kMaxN];
   int LL[(kMaxN + 1) * kMaxN];
   int LS;
-  // and of Mmat: MH/ML[i*(N+1) + r] = limbs of round(M(r,i) 2^MS), the weight of flux
-  // point r in the derivative at solution point i (the column-major index of Mmat)
+  // and of Mmat (sigma = -1, C(i, r) = M(r, i), the weight of flux point r in the
+  // derivative at solution point i: rows i < (N+1)/2 of N+1 limbs) at scale 2^MS
   int MH[(kMaxN + 1) * kMaxN];
   int ML[(kMaxN + 1) * kMaxN];
   int MS;
@@ -206,11 +207,7 @@ template <int N, class O>
 __device__ __forceinline__ void interp_line(const double (&v)[N], double (&y)[N + 1]) {
   const int emax = fix_emax(v);
   if (emax <= kFixEmaxFast) {
-    int h[N], l[N];
-    fix_align(v, emax, h, l);
-    const int sc = emax - 1017 - kFixG - O::ops().LS;
-#pragma unroll
-    for (int f = 0; f <= N; f++) y[f] = fix_dot(h, l, O::ops().LH + f * N, O::ops().LL + f * N, sc);
+    fix_apply_mirror<N + 1, N, 1>(v, emax, O::ops().LH, O::ops().LL, emax - 1017 - kFixG - O::ops().LS, y);
     return;
   }
   double ev[N / 2 > 0 ? N / 2 : 1], od[N / 2 > 0 ? N / 2 : 1];
@@ -243,11 +240,7 @@ __device__ __forceinline__ void deriv_line(const double* x, int xs, double (&y)[
   for (int r = 0; r <= N; r++) v[r] = x[r * xs];
   const int emax = fix_emax(v);
   if (emax <= kFixEmaxFast) {
-    int h[N + 1], l[N + 1];
-    fix_align(v, emax, h, l);
-    const int sc = emax - 1017 - kFixG - O::ops().MS;
-#pragma unroll
-    for (int i = 0; i < N; i++) y[i] = fix_dot(h, l, O::ops().MH + i * (N + 1), O::ops().ML + i * (N + 1), sc);
+    fix_apply_mirror<N, N + 1, -1>(v, emax, O::ops().MH, O::ops().ML, emax - 1017 - kFixG - O::ops().MS, y);
   } else {
 #pragma unroll
     for (int i = 0; i < N; i++) {
@@ -392,7 +385,7 @@ __device__ __forceinline__ void e1_body(const SolveDev& s, int e0, int cnt, int 
 
 // cells [c0, c1) of the solve, epb per CTA
 template <int N>
-__global__ void __launch_bounds__(512) k_e1(SolveDev s, int epb, int sensor, int c0, int c1) {
+__global__ void __launch_bounds__(512, 2) k_e1(SolveDev s, int epb, int sensor, int c0, int c1) {
   extern __shared__ __align__(16) double sm[];
   pdl_wait();
   // bit 4: the first pass of a stage, which starts the stage's wave-speed maximum

@@ -138,6 +138,59 @@ def test_as_accurate_as_an_fp64_chain(driver, tmp_path, name, C):
         assert correct >= 0.9 * X.shape[0] * NO
 
 
+def apply_mirror(driver, tmp_path, C, X, sigma):
+    """The mirror form (what the stage kernels run): results, and the effective operator
+    as exact rationals c / 2^S."""
+    C = np.ascontiguousarray(C, np.float64)
+    X = np.ascontiguousarray(X, np.float64)
+    NO, NI = C.shape
+    src, dst, opf = str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), str(tmp_path / "op.bin")
+    with open(src, "wb") as f:
+        f.write(struct.pack("<3i", NO, NI, X.shape[0]))
+        f.write(C.tobytes())
+        f.write(X.tobytes())
+    r = subprocess.run([driver, src, dst, str(sigma), opf], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = open(opf, "rb").read()
+    S = struct.unpack("<i", raw[:4])[0]
+    ce = np.frombuffer(raw[4:], np.int64).reshape(NO, NI)
+    return np.fromfile(dst, np.float64).reshape(X.shape[0], NO), S, ce
+
+
+MIRROR = [(name, C, 1 if name.startswith("L") else -1) for name, C in OPS]
+
+
+@pytest.mark.parametrize("name,C,sigma", MIRROR, ids=[o[0] for o in MIRROR])
+def test_mirror_form(driver, tmp_path, name, C, sigma):
+    """The mirror form pairs outputs k and NO-1-k on half the multiply-adds: its effective
+    operator is exactly (anti)symmetric, lies within 1.5 units of 2^-S plus half the given
+    operator's own mirror asymmetry (the rounding of its construction) of every coefficient,
+    and its results keep the error bound of the plain form against exact sums of it."""
+    rng = np.random.default_rng(sum(map(ord, name)) + 1)
+    NO, NI = C.shape
+    X = lines(rng, NI, 40)
+    Y, S, ce = apply_mirror(driver, tmp_path, C, X, sigma)
+    assert np.array_equal(ce[::-1, ::-1], sigma * ce)
+    unit = Fraction(1, 2 ** S)
+    asym = np.abs(C - sigma * C[::-1, ::-1]) / 2
+    assert asym.max() <= 4e-15 * np.abs(C).max()
+    Ce = [[Fraction(int(ce[k, j])) * unit for j in range(NI)] for k in range(NO)]
+    for k in range(NO):
+        for j in range(NI):
+            assert abs(Ce[k][j] - Fraction(float(C[k, j]))) <= Fraction(3, 2) * unit + Fraction(float(asym[k, j]))
+    cabs = [sum(abs(float(c)) for c in row) for row in Ce]
+    cmax = max(max(abs(float(c)) for c in row) for row in Ce)
+    for x, y in zip(X, Y):
+        xmax = np.abs(x).max()
+        for k in range(NO):
+            e = sum(c * Fraction(float(v)) for c, v in zip(Ce[k], x))
+            err = abs(Fraction(float(y[k])) - e)
+            tol = 0.5 * ulp(e) + 2.0 ** -55 * xmax * (cabs[k] + NI * cmax)
+            if xmax < 2.0 ** -960:
+                tol = max(tol, 2.0 ** -1022)
+            assert float(err) <= tol, (name, x, k, float(y[k]), float(e))
+
+
 def test_special_lines(driver, tmp_path):
     C = dict(OPS)["L5"]
     X = np.array([[np.nan, 1, 2, 3, 4], [np.inf, 0, 0, 0, 0], [1e290, 1, 1, 1, 1], [0.0] * 5, [-0.0] * 5,
