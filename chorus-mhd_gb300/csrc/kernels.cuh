@@ -507,7 +507,7 @@ __device__ __forceinline__ unsigned long long f1_point(const SolveDev& s, int t)
 // face points [t2, t2 + n2) of the two-sided list, then [t1, t1 + n - n2) of the FREE list
 // (f1_point numbering: the FREE faces follow the two-sided ones)
 template <int N>
-__global__ void __launch_bounds__(256) k_f1(SolveDev s, int t2, int n2, int t1, int n) {
+__global__ void __launch_bounds__(256, 3) k_f1(SolveDev s, int t2, int n2, int t1, int n) {
   pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long evb = 0ull;
