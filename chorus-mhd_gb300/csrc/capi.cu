@@ -161,7 +161,8 @@ constexpr int kMaxHostChunks = 32;  // chunks of a host-state upload / download
 
 constexpr int kMaxHostSegs = 2 * kMaxHostChunks + 2;
 
-// The chunks of a host-state step: cells [cut[k], cut[k+1]); two-sided faces [f2[k], f2[k+1])
+// The chunks of a host-state step: cells [cut[k], cut[k+1]) (smaller towards both ends);
+// two-sided faces [f2[k], f2[k+1])
 // (those whose larger cell is in chunk k) and FREE faces [f1[k], f1[k+1]) (cell in chunk
 // k).  The download goes by segments of cells [sb[i], se[i]) whose cells and face
 // neighbours all lie in chunks 0..sk[i]: the maximal runs of cells that complete with the
@@ -216,7 +217,7 @@ struct ChorusCtx {
   // host-state steps: a copy stream and events that chain chunked copies to kernels
   cudaStream_t cp = nullptr;
   cudaEvent_t ev[kMaxHostChunks + kMaxHostSegs + 2] = {};
-  int host_chunks = 8;  // option "host_chunks"
+  int host_chunks = 16;  // option "host_chunks"
   // the larger cell of each two-sided face and the cell of each FREE face, in list order
   // (ascending), and per cell the largest index among itself and its face neighbours
   std::vector<int> f2max, f1cell, cellrel;
@@ -790,8 +791,12 @@ const HostChunks& host_chunks(ChorusCtx* c) {
   if (h.K) return h;
   const int NC = c->sd.NC;
   h.K = std::max(1, std::min(c->host_chunks, NC / 1024));
+  // chunk sizes taper towards both ends (weights min(k+1, K-k, 4)): the first upload chunk
+  // is all the compute waits for, the last download run all that follows it
+  long long wsum[kMaxHostChunks + 1] = {0};
+  for (int k = 0; k < h.K; k++) wsum[k + 1] = wsum[k] + std::min(std::min(k + 1, h.K - k), 4);
   for (int k = 0; k <= h.K; k++) {
-    h.cut[k] = (int)((long long)NC * k / h.K);
+    h.cut[k] = (int)((long long)NC * wsum[k] / wsum[h.K]);
     h.f2[k] = (int)(std::lower_bound(c->f2max.begin(), c->f2max.end(), h.cut[k]) - c->f2max.begin());
     h.f1[k] = (int)(std::lower_bound(c->f1cell.begin(), c->f1cell.end(), h.cut[k]) - c->f1cell.begin());
   }

@@ -229,7 +229,7 @@ int chorus_gpu_profile_stage(ChorusCtx* ctx, int32_t reps, double* ms);
  *   "plot_sensor" (default 0): the last stage of each step also records the AV sensor
  *       of variable 6, which only the plot output reads (about 1% of a step); takes
  *       effect on the stream in order, without rebuilding the step graphs;
- *   "host_chunks" (1..32, default 8): chunks of cells in which chorus_gpu_step_host
+ *   "host_chunks" (1..32, default 16): chunks of cells in which chorus_gpu_step_host
  *       copies a state of 64 MB or more, each chunk's copy overlapped with the passes
  *       that can run on it (fewer for meshes under 1024 cells per chunk);
  *   "epb_e1" / "epb_e2" / "epb_e3" / "epb_ct" (1..64): cells per CTA of a cell pass;

@@ -379,11 +379,11 @@ def test_step_host_graph_cache(case_root):
 def test_host_chunks_option_range(case_root):
     d = make_case(case_root, problem="orszag_tang", nx=8, ny=8, N=3)
     s = Solver(Mesh(d))
-    assert s.get_option("host_chunks") == 8
+    assert s.get_option("host_chunks") == 16
     for bad in (0, 33):
         with pytest.raises(Exception, match="host_chunks"):
             s.set_option("host_chunks", bad)
-    assert s.get_option("host_chunks") == 8
+    assert s.get_option("host_chunks") == 16
     s.close()
 
 
