@@ -140,12 +140,13 @@ static const Dispatch* dispatch_for(int N) {
 // default launch shapes per N (cells per CTA, threads per CTA)
 Launch default_launch(int N, int which) {
   // which: 0 = E1, 1 = E2, 2 = E3, 3 = CT; cells per CTA and threads per CTA as the
-  // autotuner picked them on GB300 for N = 3..6; the CT passes take about 128/(2N) cells
+  // autotuner picked them on GB300 for N = 3..6 (for N = 6 the shapes of an earlier tuning,
+  // which the batched form runs faster); the CT passes take about 128/(2N) cells
   // so that their (cell, line) loop fills the 128 threads
   static const int epb[kMaxN + 1][4] = {{0}, {0}, {16, 16, 16, 32}, {16, 4, 2, 21}, {4, 4, 4, 16},
-                                        {4, 2, 5, 12}, {8, 2, 2, 10}, {2, 2, 2, 9}, {2, 2, 2, 8}};
+                                        {4, 2, 5, 12}, {3, 2, 2, 10}, {2, 2, 2, 9}, {2, 2, 2, 8}};
   static const int thr[kMaxN + 1][4] = {{0}, {0}, {128, 128, 128, 128}, {224, 128, 32, 128}, {128, 128, 96, 128},
-                                        {128, 128, 160, 128}, {320, 96, 64, 128}, {128, 128, 128, 128},
+                                        {128, 128, 160, 128}, {96, 192, 128, 128}, {128, 128, 128, 128},
                                         {128, 128, 128, 128}};
   return Launch{epb[N][which], thr[N][which]};
 }
