@@ -95,6 +95,7 @@ SIGNATURES = {
     "chorus_batch_info": (c_int, [c_void_p, ip, ip, ip, P(ctypes.c_int64)]),
     "chorus_serve_run": (c_int, [P(ChorusServeRequest), c_int, P(ChorusServeConfig), P(ChorusServeResult), dp]),
     "chorus_mesh_device_bytes": (ctypes.c_int64, [c_void_p]),
+    "chorus_mesh_host_chunks": (c_int, [c_void_p, c_int, ip, ip, ip, ip, ip, ip]),
     "chorus_mesh_load": (c_int, [c_char_p, P(c_void_p)]),
     "chorus_mesh_load_gpu": (c_int, [c_char_p, c_int, P(c_void_p)]),
     "chorus_mesh_free": (c_int, [c_void_p]),

@@ -787,19 +787,20 @@ void enqueue_diag(ChorusCtx* c) {
   k_store_record<<<1, 1, 0, c->st>>>(c->red, c->sd.eig, c->red + 4);
 }
 
-const HostChunks& host_chunks(ChorusCtx* c) {
-  HostChunks& h = c->hc;
-  if (h.K) return h;
-  const int NC = c->sd.NC;
-  h.K = std::max(1, std::min(c->host_chunks, NC / 1024));
+// the chunk plan of a host-state step from the keys of the face lists: the larger cell of
+// each two-sided face and the cell of each FREE face (both ascending), and per cell the
+// largest index among itself and its face neighbours
+void plan_host_chunks(int NC, int chunks, const std::vector<int>& f2max, const std::vector<int>& f1cell,
+                      const std::vector<int>& cellrel, HostChunks& h) {
+  h.K = std::max(1, std::min(chunks, NC / 1024));
   // chunk sizes taper towards both ends (weights min(k+1, K-k, 4)): the first upload chunk
   // is all the compute waits for, the last download run all that follows it
   long long wsum[kMaxHostChunks + 1] = {0};
   for (int k = 0; k < h.K; k++) wsum[k + 1] = wsum[k] + std::min(std::min(k + 1, h.K - k), 4);
   for (int k = 0; k <= h.K; k++) {
     h.cut[k] = (int)((long long)NC * wsum[k] / wsum[h.K]);
-    h.f2[k] = (int)(std::lower_bound(c->f2max.begin(), c->f2max.end(), h.cut[k]) - c->f2max.begin());
-    h.f1[k] = (int)(std::lower_bound(c->f1cell.begin(), c->f1cell.end(), h.cut[k]) - c->f1cell.begin());
+    h.f2[k] = (int)(std::lower_bound(f2max.begin(), f2max.end(), h.cut[k]) - f2max.begin());
+    h.f1[k] = (int)(std::lower_bound(f1cell.begin(), f1cell.end(), h.cut[k]) - f1cell.begin());
   }
   // the chunk that completes each cell's neighbourhood (cellrel >= the cell itself)
   auto chunk_of = [&](int ic) {
@@ -807,9 +808,9 @@ const HostChunks& host_chunks(ChorusCtx* c) {
   };
   h.nseg = 0;
   for (int ic = 0; ic < NC;) {
-    const int k = chunk_of(c->cellrel[ic]);
+    const int k = chunk_of(cellrel[ic]);
     int e = ic + 1;
-    while (e < NC && chunk_of(c->cellrel[e]) == k) e++;
+    while (e < NC && chunk_of(cellrel[e]) == k) e++;
     if (h.nseg == kMaxHostSegs) {
       h.nseg = -1;
       break;
@@ -824,13 +825,17 @@ const HostChunks& host_chunks(ChorusCtx* c) {
     h.nseg = h.K;
     for (int j = 0; j < h.K; j++) {
       int r = h.cut[j + 1] - 1;
-      for (int ic = h.cut[j]; ic < h.cut[j + 1]; ic++) r = std::max(r, c->cellrel[ic]);
+      for (int ic = h.cut[j]; ic < h.cut[j + 1]; ic++) r = std::max(r, cellrel[ic]);
       h.sb[j] = h.cut[j];
       h.se[j] = h.cut[j + 1];
       h.sk[j] = chunk_of(r);
     }
   }
-  return h;
+}
+
+const HostChunks& host_chunks(ChorusCtx* c) {
+  if (!c->hc.K) plan_host_chunks(c->sd.NC, c->host_chunks, c->f2max, c->f1cell, c->cellrel, c->hc);
+  return c->hc;
 }
 
 // One step whose state comes from / goes to host memory, the copies (on the copy stream,
@@ -1558,6 +1563,43 @@ int64_t chorus_mesh_device_bytes(const ChorusMesh* mh) {
   const Mesh& m = mh->m;
   const int nface2 = (int)m.IBFINTER.size() + m.NPAIR, nface1 = (int)m.IBFREE.size();
   return (int64_t)arena_plan_bytes(m.N, m.NCELL, nface2, nface1, m.params.k_stage);
+}
+
+int chorus_mesh_host_chunks(const ChorusMesh* mh, int32_t chunks, int32_t* K, int32_t* cut, int32_t* f2cut,
+                            int32_t* f1cut, int32_t* nseg, int32_t* seg) {
+  if (!mh || !K || !cut || !f2cut || !f1cut || !nseg || !seg) return set_err(CHORUS_EINVAL, "null argument");
+  if (chunks < 1 || chunks > kMaxHostChunks)
+    return set_err(CHORUS_EINVAL, "chunks=%d outside 1..%d", (int)chunks, kMaxHostChunks);
+  const Mesh& m = mh->m;
+  const int NC = m.NCELL, NF = m.NFACE;
+  // the keys the bound context computes from its face lists (chorus_gpu_bind)
+  std::vector<int> f2max, f1cell, rel(NC);
+  for (int ic = 0; ic < NC; ic++) rel[ic] = ic;
+  auto two = [&](int cl, int cr) {
+    f2max.push_back(std::max(cl, cr));
+    rel[cl] = std::max(rel[cl], cr);
+    rel[cr] = std::max(rel[cr], cl);
+  };
+  for (int32_t f1 : m.IBFINTER) two(m.IF2C[f1 - 1] - 1, m.IF2C[f1 - 1 + NF] - 1);
+  for (int i = 0; i < m.NPAIR; i++) two(m.IF2C[m.CYC2FPAIR[i] - 1] - 1, m.IF2C[m.CYC2FPAIR[i + m.NPAIR] - 1] - 1);
+  for (int32_t f1 : m.IBFREE) f1cell.push_back(m.IF2C[f1 - 1] - 1);
+  std::sort(f2max.begin(), f2max.end());
+  std::sort(f1cell.begin(), f1cell.end());
+  HostChunks h;
+  plan_host_chunks(NC, chunks, f2max, f1cell, rel, h);
+  *K = h.K;
+  for (int k = 0; k <= h.K; k++) {
+    cut[k] = h.cut[k];
+    f2cut[k] = h.f2[k];
+    f1cut[k] = h.f1[k];
+  }
+  *nseg = h.nseg;
+  for (int i = 0; i < h.nseg; i++) {
+    seg[3 * i] = h.sb[i];
+    seg[3 * i + 1] = h.se[i];
+    seg[3 * i + 2] = h.sk[i];
+  }
+  return CHORUS_OK;
 }
 
 int chorus_gpu_bind_mesh(const ChorusMesh* mh, int32_t device, ChorusCtx** ctx) {

@@ -314,6 +314,15 @@ int chorus_serve_run(const ChorusServeRequest* reqs, int32_t n, const ChorusServ
                      ChorusServeResult* results, double* makespan_s);
 /* Device bytes chorus_gpu_bind_mesh would allocate for this mesh (admission control). */
 int64_t chorus_mesh_device_bytes(const ChorusMesh* mesh);
+/* The chunk plan chorus_gpu_step_host follows for this mesh with the option host_chunks =
+ * chunks (host only; for inspection and tests): *K chunks of cells [cut[k], cut[k+1])
+ * (K+1 entries, at most 33); the two-sided faces [f2cut[k], f2cut[k+1]) of the face list in
+ * the order of its larger cell, i.e. those whose larger cell is in chunk k, and the FREE
+ * faces [f1cut[k], f1cut[k+1]) in cell order; *nseg download runs (at most 66) as
+ * seg[3i], seg[3i+1], seg[3i+2] = first cell, end cell, and the chunk after whose last-stage
+ * passes all of the run's cells and their face neighbours are final. */
+int chorus_mesh_host_chunks(const ChorusMesh* mesh, int32_t chunks, int32_t* K, int32_t* cut, int32_t* f2cut,
+                            int32_t* f1cut, int32_t* nseg, int32_t* seg);
 
 /* ------------------------------------------------------------------------------
  * Host-side setup for callers without the Fortran setup chain: reads QUAD.INP and
