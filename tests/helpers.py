@@ -19,6 +19,28 @@ def make_case(root, **kw):
     return _CACHE[key]
 
 
+def shuffled_case(root, order_seed, **kw):
+    """The case of CaseSpec(**kw) with its cells listed in a seeded random order (the mesh
+    reader numbers cells by their line in the .CEL file), i.e. the same mesh with scattered
+    cell numbers; written once per session."""
+    import shutil
+    key = ("shuffled", order_seed) + tuple(sorted(kw.items()))
+    if key not in _CACHE:
+        src = make_case(root, **kw)
+        d = src + "_shuffled%d" % order_seed
+        if os.path.exists(d):
+            shutil.rmtree(d)
+        shutil.copytree(src, d)
+        cel = os.path.join(d, "mesh.CEL")
+        lines = open(cel).read().splitlines()
+        order = np.random.default_rng(order_seed).permutation(len(lines))
+        with open(cel, "w") as f:
+            for i, j in enumerate(order, 1):
+                f.write("%8d%s\n" % (i, lines[j][8:]))
+        _CACHE[key] = d
+    return _CACHE[key]
+
+
 def rel_l2(a, b):
     a = np.asarray(a, np.float64).ravel()
     b = np.asarray(b, np.float64).ravel()

@@ -9,7 +9,7 @@ import pytest
 
 import oracle
 from chorus_mhd import Mesh, Solver, reference_layout_sizes
-from helpers import alfven_wave_bz, alfven_wave_case, diffusion_wave_case, entropy_wave_case, entropy_wave_state, quadrature_l2, assert_close, make_case, rel_l2
+from helpers import alfven_wave_bz, alfven_wave_case, diffusion_wave_case, entropy_wave_case, entropy_wave_state, quadrature_l2, assert_close, make_case, rel_l2, shuffled_case
 
 pytestmark = pytest.mark.gpu
 
@@ -372,6 +372,25 @@ def test_step_host_graph_cache(case_root):
         assert np.array_equal(buf, q), "step %d" % (k + 1)
     assert b.iter == a.iter and b.ctime == a.ctime
     assert [r["residglob"] for r in b.diagnostics] == [r["residglob"] for r in a.diagnostics]
+    a.close()
+    b.close()
+
+
+def test_step_host_on_scattered_cell_numbering(case_root):
+    """Cells numbered in a random order: nearly every cell has a face neighbour in the last
+    chunk, so the chunk plan downloads whole chunks, each once its last neighbour is through;
+    the host-state step still gives the resident steps' bits."""
+    torch = pytest.importorskip("torch")
+    d = shuffled_case(case_root, 3, problem="orszag_tang", nx=256, ny=240, N=4, jitter=0.1, seed=21)
+    a = Solver(Mesh(d))
+    q0 = a.state()
+    a.iterations(2)
+    ref = a.state()
+    pin = torch.empty(q0.size, dtype=torch.float64, pin_memory=True).numpy()
+    pin[:] = q0
+    b = Solver(Mesh(d))
+    b.step_host(pin, pin, 2)
+    assert np.array_equal(pin, ref)
     a.close()
     b.close()
 

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from chorus_mhd import Mesh, _lib
-from helpers import make_case
+from helpers import make_case, shuffled_case
 
 CASES = [dict(problem="orszag_tang", nx=72, ny=64, N=4, jitter=0.1, seed=21),
          dict(problem="orszag_tang", nx=256, ny=240, N=4, jitter=0.1, seed=21),
@@ -44,14 +44,17 @@ def faces(mesh):
 
 @pytest.fixture(scope="module")
 def meshes(tmp_path_factory):
-    root = tmp_path_factory.mktemp("chunks")
-    out = [Mesh(make_case(str(root), **c)) for c in CASES]
+    """The cases above, then the periodic 256x240 case and the rotor with their cells
+    numbered in a random order (the plan's fallback to whole chunks)."""
+    root = str(tmp_path_factory.mktemp("chunks"))
+    out = [Mesh(make_case(root, **c)) for c in CASES]
+    out += [Mesh(shuffled_case(root, 3, **CASES[1])), Mesh(shuffled_case(root, 4, **CASES[2]))]
     yield out
     for m in out:
         m.close()
 
 
-@pytest.mark.parametrize("which", range(len(CASES)))
+@pytest.mark.parametrize("which", range(len(CASES) + 2))
 @pytest.mark.parametrize("chunks", [1, 3, 8, 16, 32])
 def test_plan_respects_face_dependencies(meshes, which, chunks):
     m = meshes[which]
@@ -88,6 +91,16 @@ def test_plan_releases_runs_with_their_chunk(meshes):
         K, cut, _, _, seg = plan(m, 16)
         early = sum(b - a for a, b, k in seg if k < K - 1)
         assert early >= 0.8 * m.ncell
+
+
+def test_scattered_numbering_falls_back_to_whole_chunks(meshes):
+    """With cells numbered at random nearly every cell has a neighbour in the last chunk, so
+    the runs fragment and the plan downloads whole chunks, each when its last neighbour is
+    through (still checked above)."""
+    for m in meshes[len(CASES):]:
+        K, cut, _, _, seg = plan(m, 16)
+        assert len(seg) == K
+        assert np.array_equal(seg[:, 0], cut[:-1]) and np.array_equal(seg[:, 1], cut[1:])
 
 
 def test_plan_rejects_bad_counts(meshes):
